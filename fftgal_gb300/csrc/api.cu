@@ -1,0 +1,986 @@
+// C ABI of libfftgal_gb300.so: the reference's fft.h / power.h functions
+// (src/fft.h:27-49, src/power.h:7-13) on a GPU-resident grid, plus the
+// extensions of include/fftgal_gb300.h.
+//
+// Each fft_t owns: the canonical grid in HBM (FP32 or FP64), a second grid for
+// interlacing, FFT plans, paint tiling and scratch, spectral tables, the
+// binning geometry cache and a CUDA stream.  The reference's `f` stays a host
+// double array: under the "sync" host view it mirrors the device grid after
+// every call (and is re-read at the start of every call that reads the grid),
+// under "lazy" it is refreshed only on request.  Errors in reference-API calls
+// print a message and abort(), as the reference's assert() does.
+#include "internal.h"
+#include "common.cuh"
+
+#include "fft.h"
+#include "power.h"
+#include "fftgal_gb300.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <atomic>
+#include <chrono>
+#include <vector>
+
+namespace fg {
+
+// ---- errors ----------------------------------------------------------------------
+static thread_local int t_status = 0;
+static thread_local char t_msg[1024] = "";
+
+int set_error(int status, const char *fmt, ...) {
+    t_status = status;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_msg, sizeof(t_msg), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+int cuda_check(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return OK;
+    return set_error(e == cudaErrorMemoryAllocation ? ERR_NOMEM : ERR_CUDA, "%s: %s", what,
+                     cudaGetErrorString(e));
+}
+
+static std::atomic<long> g_launches{0};
+void note_launches(int n) { g_launches += n; }
+long launch_count() { return g_launches.load(); }
+
+int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+int device_max_smem() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+// ---- per-grid device state -----------------------------------------------------------
+constexpr int kGeoCache = 8;
+// timed stages of fftgal_power_f32: upload, key, scan, scatter, paint tile,
+// fft k, fft j, fft i, finish (phase/average/deconv), bin
+constexpr int kStages = 10;
+
+struct Grid {
+    int prec = 4;
+    int Ng = 0, Ng_pad = 0, nh = 0;
+    long Ng3_pad = 0;
+    double L = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    void *d_f = nullptr, *d_aux = nullptr;
+    int view = FFTGAL_VIEW_SYNC;
+    bool pinned = false;
+    int quiet = 0;
+    FftPlan fft;
+    PaintTiling tiling;
+    PaintScratch scratch;
+    void *d_pos = nullptr;  // 3 position arrays (float or double)
+    size_t pos_cap = 0;     // bytes
+    void *d_stage = nullptr;  // host-double staging for uploads
+    size_t stage_cap = 0;
+    double *d_tab = nullptr;  // [3][Ng] complex phase table + [Ng] winv
+    BinGeometry geo[kGeoCache];
+    int geo_next = 0;
+    unsigned long version = 1;  // bumped whenever the grid changes
+    // Pl -> Pmu reuse of the wedge sums from the same pass
+    struct {
+        unsigned long version = 0;
+        BinSpec spec;
+        std::vector<double> Pw;
+    } wedge_cache;
+    int timing = 0;
+    cudaEvent_t ev[kStages + 1] = {};
+    double stage_ms[kStages + 1] = {};
+};
+
+static Grid *G(const fft_t *f) { return f ? reinterpret_cast<Grid *>(f->x2k) : nullptr; }
+
+static int env_precision() {
+    const char *e = getenv("FFTGAL_PRECISION");
+    if (!e) return 4;
+    if (!strcmp(e, "f64") || !strcmp(e, "fp64") || !strcmp(e, "double") || !strcmp(e, "8")) return 8;
+    return 4;
+}
+
+static int env_view() {
+    const char *e = getenv("FFTGAL_HOST_VIEW");
+    return (e && !strcmp(e, "lazy")) ? FFTGAL_VIEW_LAZY : FFTGAL_VIEW_SYNC;
+}
+
+static int env_quiet() {
+    const char *e = getenv("FFTGAL_QUIET");
+    return e && strcmp(e, "0") != 0;
+}
+
+[[noreturn]] static void die(const char *where) {
+    fprintf(stderr, "%s: %s\n", where, t_msg[0] ? t_msg : "failure");
+    fflush(stderr);
+    abort();
+}
+
+#define FG_API(expr, where)              \
+    do {                                 \
+        if ((expr) != 0) die(where);     \
+    } while (0)
+
+static double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ---- host view transfers -----------------------------------------------------------------
+constexpr size_t kStageBytes = 64u << 20;
+
+static int ensure_stage(Grid *g, size_t bytes) {
+    if (bytes <= g->stage_cap) return OK;
+    cudaFree(g->d_stage);
+    g->d_stage = nullptr;
+    FG_CUDA(cudaMalloc(&g->d_stage, bytes));
+    g->stage_cap = bytes;
+    return OK;
+}
+
+// device grid -> host double array (pinned: direct conversion; else staged)
+static int device_to_host(Grid *g, double *host, bool host_pinned) {
+    if (g->prec == 8) {
+        FG_CUDA(cudaMemcpyAsync(host, g->d_f, sizeof(double) * g->Ng3_pad, cudaMemcpyDeviceToHost, g->stream));
+    } else if (host_pinned) {
+        FG_TRY(convert_grid(host, 8, g->d_f, 4, g->Ng3_pad, g->stream));
+    } else {
+        FG_TRY(ensure_stage(g, kStageBytes));
+        const long chunk = kStageBytes / 8;
+        for (long o = 0; o < g->Ng3_pad; o += chunk) {
+            const long n = g->Ng3_pad - o < chunk ? g->Ng3_pad - o : chunk;
+            FG_TRY(convert_grid(g->d_stage, 8, (const float *)g->d_f + o, 4, n, g->stream));
+            FG_CUDA(cudaMemcpyAsync(host + o, g->d_stage, sizeof(double) * n, cudaMemcpyDeviceToHost, g->stream));
+        }
+    }
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    return OK;
+}
+
+static int host_to_device(Grid *g, const double *host, bool host_pinned) {
+    if (g->prec == 8) {
+        FG_CUDA(cudaMemcpyAsync(g->d_f, host, sizeof(double) * g->Ng3_pad, cudaMemcpyHostToDevice, g->stream));
+    } else if (host_pinned) {
+        FG_TRY(convert_grid(g->d_f, 4, host, 8, g->Ng3_pad, g->stream));
+    } else {
+        FG_TRY(ensure_stage(g, kStageBytes));
+        const long chunk = kStageBytes / 8;
+        for (long o = 0; o < g->Ng3_pad; o += chunk) {
+            const long n = g->Ng3_pad - o < chunk ? g->Ng3_pad - o : chunk;
+            FG_CUDA(cudaMemcpyAsync(g->d_stage, host + o, sizeof(double) * n, cudaMemcpyHostToDevice, g->stream));
+            FG_TRY(convert_grid((float *)g->d_f + o, 4, g->d_stage, 8, n, g->stream));
+        }
+    }
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    ++g->version;
+    return OK;
+}
+
+// entry/exit of reference-API calls under the host-view policy
+static int enter(fft_t *self, bool reads_grid) {
+    Grid *g = G(self);
+    if (g->view == FFTGAL_VIEW_SYNC && reads_grid) FG_TRY(host_to_device(g, self->f, g->pinned));
+    return OK;
+}
+
+static int leave(fft_t *self, bool modified) {
+    Grid *g = G(self);
+    if (modified) ++g->version;
+    if (g->view == FFTGAL_VIEW_SYNC && modified) FG_TRY(device_to_host(g, self->f, g->pinned));
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    return OK;
+}
+
+// ---- helpers ------------------------------------------------------------------------------
+static int ensure_aux(Grid *g) {
+    if (g->d_aux) return OK;
+    FG_CUDA(cudaMalloc(&g->d_aux, (size_t)g->prec * g->Ng3_pad));
+    return OK;
+}
+
+static int ensure_tables(Grid *g) {
+    if (g->d_tab) return OK;
+    FG_CUDA(cudaMalloc(&g->d_tab, sizeof(double) * (7 * (size_t)g->Ng)));
+    std::vector<double> w(g->Ng);
+    build_winv_table(w.data(), g->Ng);
+    FG_CUDA(cudaMemcpy(g->d_tab + 6 * (size_t)g->Ng, w.data(), sizeof(double) * g->Ng, cudaMemcpyHostToDevice));
+    return OK;
+}
+
+static int phase(Grid *g, void *dst, const double offset[3], int onoff) {
+    FG_TRY(ensure_tables(g));
+    std::vector<double> tab(6 * (size_t)g->Ng);
+    build_phase_table(tab.data(), g->Ng, offset, onoff);
+    FG_CUDA(cudaMemcpyAsync(g->d_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, g->stream));
+    FG_TRY(apply_phase(dst, g->Ng, g->prec, g->d_tab, g->stream));
+    // the host table must outlive the async copy
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    return OK;
+}
+
+static int deconv(Grid *g, void *dst) {
+    FG_TRY(ensure_tables(g));
+    return apply_deconv(dst, g->Ng, g->prec, g->d_tab + 6 * (size_t)g->Ng, g->stream);
+}
+
+// positions of a catalog (host doubles) -> device arrays in the grid's precision
+static int upload_positions(Grid *g, const gal_t *part, void **px, void **py, void **pz) {
+    const long Np = part->Np;
+    const size_t need = (size_t)3 * (Np > 0 ? Np : 1) * g->prec;
+    if (need > g->pos_cap) {
+        cudaFree(g->d_pos);
+        g->d_pos = nullptr;
+        FG_CUDA(cudaMalloc(&g->d_pos, need));
+        g->pos_cap = need;
+    }
+    char *base = (char *)g->d_pos;
+    const double *src[3] = {part->x, part->y, part->z};
+    void *dst[3];
+    for (int a = 0; a < 3; ++a) dst[a] = base + (size_t)a * (Np > 0 ? Np : 1) * g->prec;
+    if (Np > 0) {
+        if (g->prec == 8) {
+            for (int a = 0; a < 3; ++a)
+                FG_CUDA(cudaMemcpyAsync(dst[a], src[a], sizeof(double) * Np, cudaMemcpyHostToDevice, g->stream));
+        } else {
+            FG_TRY(ensure_stage(g, kStageBytes));
+            const long chunk = kStageBytes / 8;
+            for (int a = 0; a < 3; ++a)
+                for (long o = 0; o < Np; o += chunk) {
+                    const long n = Np - o < chunk ? Np - o : chunk;
+                    FG_CUDA(cudaMemcpyAsync(g->d_stage, src[a] + o, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                            g->stream));
+                    FG_TRY(convert_grid((float *)dst[a] + o, 4, g->d_stage, 8, n, g->stream));
+                }
+        }
+    }
+    *px = dst[0];
+    *py = dst[1];
+    *pz = dst[2];
+    return OK;
+}
+
+// paint `part` (and its randoms) onto the given grids of the same tiling
+static int paint_catalog(Grid *g, const gal_t *part, void *const *outs, double (*offs)[3], int ngrids) {
+    void *x, *y, *z;
+    FG_TRY(upload_positions(g, part, &x, &y, &z));
+    const double Hinv = g->Ng / g->L;
+    const double H = g->L / g->Ng;
+    const double H3r = H * H * H;  // gsl_pow_3(L/Ng) as the reference evaluates it
+    const double nbar = part->Np / part->V;
+    const double Npcinv = 1 / nbar / H3r;
+    PaintGridSpec spec[2];
+    for (int q = 0; q < ngrids; ++q) {
+        spec[q].out = outs[q];
+        for (int a = 0; a < 3; ++a) spec[q].offset[a] = offs[q][a];
+        spec[q].scale = Npcinv;
+        spec[q].accumulate = 0;
+    }
+    FG_TRY(paint(&g->tiling, &g->scratch, g->prec, x, y, z, g->prec, part->Np, Hinv, spec, ngrids, g->stream));
+    if (part->rand) {
+        const gal_t *r = part->rand;
+        const double alpha = (double)part->Np / r->Np;
+        FG_TRY(upload_positions(g, r, &x, &y, &z));
+        for (int q = 0; q < ngrids; ++q) {
+            spec[q].scale = -alpha * Npcinv;
+            spec[q].accumulate = 1;
+        }
+        FG_TRY(paint(&g->tiling, &g->scratch, g->prec, x, y, z, g->prec, r->Np, Hinv, spec, ngrids, g->stream));
+    }
+    return OK;
+}
+
+static double H3_of(const Grid *g) {
+    const double H = g->L / g->Ng;
+    return H * H * H;
+}
+
+static BinGeometry *geometry(Grid *g, const BinSpec &s) {
+    for (int q = 0; q < kGeoCache; ++q) {
+        BinGeometry &c = g->geo[q];
+        if (c.valid && c.spec.Ng == s.Ng && c.spec.L == s.L && c.spec.dK == s.dK && c.spec.Nmu == s.Nmu &&
+            c.spec.los[0] == s.los[0] && c.spec.los[1] == s.los[1] && c.spec.los[2] == s.los[2])
+            return &c;
+    }
+    BinGeometry &c = g->geo[g->geo_next];
+    g->geo_next = (g->geo_next + 1) % kGeoCache;
+    if (bin_geometry_build(&c, s, g->stream) != OK) return nullptr;
+    return &c;
+}
+
+}  // namespace fg
+
+using namespace fg;
+
+// ======================================================================================
+// reference API: src/fft.h
+// ======================================================================================
+
+extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
+    fprintf(stderr, "fft_init() making a %d^3 grid in a %g^3 box\n", Ng, L);
+    if (Ng < 2) {
+        set_error(ERR_ARG, "Ng must be >= 2");
+        die("fft_init()");
+    }
+    fft_t *self = (fft_t *)malloc(sizeof(fft_t));
+    if (!self) die("fft_init()");
+    Grid *g = new Grid();
+    self->x2k = g;
+    self->k2x = nullptr;
+    self->Ng = Ng;
+    self->L = L;
+    for (int i = 0; i < 3; ++i) self->offset[i] = 0;
+    self->Ng_pad = 2 * (Ng / 2 + 1);
+    self->Ng3_pad = (long)Ng * Ng * self->Ng_pad;
+    g->prec = env_precision();
+    g->view = env_view();
+    g->quiet = env_quiet();
+    g->Ng = Ng;
+    g->Ng_pad = self->Ng_pad;
+    g->nh = Ng / 2 + 1;
+    g->Ng3_pad = self->Ng3_pad;
+    g->L = L;
+    FG_API(cuda_check(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking), "stream"), "fft_init()");
+    g->stream = g->own_stream;
+    // host view: pinned so the GPU converts straight into it
+    void *hv = nullptr;
+    if (cudaMallocHost(&hv, sizeof(double) * self->Ng3_pad) == cudaSuccess) {
+        g->pinned = true;
+    } else {
+        cudaGetLastError();
+        hv = malloc(sizeof(double) * self->Ng3_pad);
+        if (!hv) {
+            set_error(ERR_NOMEM, "host view of %ld doubles", self->Ng3_pad);
+            die("fft_init()");
+        }
+    }
+    self->f = (double *)hv;
+    memset(self->f, 0, sizeof(double) * self->Ng3_pad);
+    FG_API(cuda_check(cudaMalloc(&g->d_f, (size_t)g->prec * self->Ng3_pad), "grid"), "fft_init()");
+    FG_API(cuda_check(cudaMemsetAsync(g->d_f, 0, (size_t)g->prec * self->Ng3_pad, g->stream), "grid"), "fft_init()");
+    FG_API(fft_plan_create(&g->fft, Ng, g->prec), "fft_init()");
+    FG_API(paint_tiling_create(&g->tiling, Ng, 16), "fft_init()");
+    FG_API(cuda_check(cudaStreamSynchronize(g->stream), "init"), "fft_init()");
+    const bool estimate = wisdom && !strcmp(wisdom, "FFTW_ESTIMATE");
+    if (estimate) {
+        fprintf(stderr, "fft_init() using built-in GPU plans (%s grid)\n", g->prec == 4 ? "FP32" : "FP64");
+    } else if (wisdom) {
+        FILE *fp = fopen(wisdom, "r");
+        if (fp) {
+            fclose(fp);
+            fprintf(stderr, "fft_init() found plan file %s\n", wisdom);
+        } else {
+            fp = fopen(wisdom, "w");
+            if (fp) {
+                fprintf(fp, "fftgal_gb300 plan Ng=%d prec=%d cols=%d rows=%d tile=%d\n", Ng, g->prec,
+                        g->fft.cols, g->fft.rows, g->tiling.tmax);
+                fclose(fp);
+                fprintf(stderr, "fft_init() exported plan to %s\n", wisdom);
+            }
+        }
+    }
+    return self;
+}
+
+extern "C" void fft_free(fft_t *self) {
+    if (self != NULL) {
+        Grid *g = G(self);
+        if (g) {
+            cudaStreamSynchronize(g->stream);
+            cudaFree(g->d_f);
+            cudaFree(g->d_aux);
+            cudaFree(g->d_pos);
+            cudaFree(g->d_stage);
+            cudaFree(g->d_tab);
+            fft_plan_destroy(&g->fft);
+            paint_tiling_destroy(&g->tiling);
+            paint_scratch_free(&g->scratch);
+            for (int q = 0; q < kGeoCache; ++q) bin_geometry_free(&g->geo[q]);
+            for (auto &e : g->ev)
+                if (e) cudaEventDestroy(e);
+            if (g->own_stream) cudaStreamDestroy(g->own_stream);
+            if (g->pinned)
+                cudaFreeHost(self->f);
+            else
+                free(self->f);
+            delete g;
+        }
+    }
+    free(self);
+}
+
+extern "C" void fft_p2g(fft_t *self, gal_t *part, double offset[3]) {
+    const double t = now_s();
+    Grid *g = G(self);
+    const int Ng = self->Ng;
+    for (int i = 0; i < 3; ++i) {
+        offset[i] = remainder(offset[i], Ng);
+        self->offset[i] = offset[i];
+    }
+    FG_API(enter(self, false), "fft_p2g()");
+    void *outs[1] = {g->d_f};
+    double offs[1][3] = {{offset[0], offset[1], offset[2]}};
+    FG_API(paint_catalog(g, part, outs, offs, 1), "fft_p2g()");
+    FG_API(leave(self, true), "fft_p2g()");
+    if (!g->quiet) fprintf(stderr, "fft_p2g() %.2fs\n", now_s() - t);
+}
+
+extern "C" void fft_x2k(fft_t *self, int offset_phase_on) {
+    const double t = now_s();
+    Grid *g = G(self);
+    FG_API(enter(self, true), "fft_x2k()");
+    void *grids[1] = {g->d_f};
+    FG_API(fft_r2c(&g->fft, grids, 1, g->stream), "fft_x2k()");
+    FG_API(scale_grid(g->d_f, self->Ng3_pad, g->prec, H3_of(g), g->stream), "fft_x2k()");
+    if (offset_phase_on) FG_API(phase(g, g->d_f, self->offset, 1), "fft_x2k()");
+    FG_API(leave(self, true), "fft_x2k()");
+    if (!g->quiet) fprintf(stderr, "fft_x2k() %.2fs\n", now_s() - t);
+}
+
+extern "C" void fft_k2x(fft_t *self, int offset_phase_off) {
+    const double t = now_s();
+    Grid *g = G(self);
+    FG_API(enter(self, true), "fft_k2x()");
+    void *grids[1] = {g->d_f};
+    FG_API(fft_c2r(&g->fft, grids, 1, g->stream), "fft_k2x()");
+    const double L3 = self->L * self->L * self->L;
+    FG_API(scale_grid(g->d_f, self->Ng3_pad, g->prec, 1 / L3, g->stream), "fft_k2x()");
+    if (offset_phase_off) FG_API(phase(g, g->d_f, self->offset, -1), "fft_k2x()");
+    FG_API(leave(self, true), "fft_k2x()");
+    if (!g->quiet) fprintf(stderr, "fft_k2x() %.2fs\n", now_s() - t);
+}
+
+extern "C" void fft_offset_phase(fft_t *self, int onoff) {
+    if (onoff == 0) {
+        set_error(ERR_ARG, "onoff must be nonzero");
+        die("fft_offset_phase()");
+    }
+    Grid *g = G(self);
+    FG_API(enter(self, true), "fft_offset_phase()");
+    FG_API(phase(g, g->d_f, self->offset, onoff), "fft_offset_phase()");
+    FG_API(leave(self, true), "fft_offset_phase()");
+}
+
+extern "C" void fft_deconv(fft_t *self) {
+    const double t = now_s();
+    Grid *g = G(self);
+    FG_API(enter(self, true), "fft_deconv()");
+    FG_API(deconv(g, g->d_f), "fft_deconv()");
+    FG_API(leave(self, true), "fft_deconv()");
+    if (!g->quiet) fprintf(stderr, "fft_deconv() %.2fs\n", now_s() - t);
+}
+
+extern "C" void fft_p2k(fft_t *self, gal_t *part) {
+    Grid *g = G(self);
+    if (!g->quiet) fprintf(stderr, "fft_p2k() interlacing\n");
+    const double t = now_s();
+    FG_API(enter(self, false), "fft_p2k()");
+    FG_API(ensure_aux(g), "fft_p2k()");
+    // both interlacing grids painted in one particle pass: offset 0 -> f,
+    // offset 1/2 -> aux (src/fft.c:260-269)
+    const int Ng = self->Ng;
+    double offs[2][3] = {{0, 0, 0}, {0.5, 0.5, 0.5}};
+    for (int q = 0; q < 2; ++q)
+        for (int a = 0; a < 3; ++a) offs[q][a] = remainder(offs[q][a], Ng);
+    void *outs[2] = {g->d_f, g->d_aux};
+    FG_API(paint_catalog(g, part, outs, offs, 2), "fft_p2k()");
+    FG_API(fft_r2c(&g->fft, outs, 2, g->stream), "fft_p2k()");
+    const double H3 = H3_of(g);
+    FG_API(scale_grid(g->d_aux, self->Ng3_pad, g->prec, H3, g->stream), "fft_p2k()");
+    FG_API(phase(g, g->d_aux, offs[1], 1), "fft_p2k()");
+    FG_API(scale_grid(g->d_f, self->Ng3_pad, g->prec, H3, g->stream), "fft_p2k()");
+    FG_API(interlace_average(g->d_f, g->d_aux, self->Ng3_pad, g->prec, g->stream), "fft_p2k()");
+    FG_API(deconv(g, g->d_f), "fft_p2k()");
+    for (int a = 0; a < 3; ++a) self->offset[a] = offs[0][a];
+    FG_API(leave(self, true), "fft_p2k()");
+    if (!g->quiet) fprintf(stderr, "fft_p2k() %.2fs\n", now_s() - t);
+}
+
+extern "C" double *fft_exportf(fft_t *self) {
+    Grid *g = G(self);
+    double *dest = (double *)malloc(self->Ng3_pad * sizeof(double));
+    if (!dest) {
+        set_error(ERR_NOMEM, "export buffer");
+        die("fft_exportf()");
+    }
+    if (g->view == FFTGAL_VIEW_SYNC)
+        memcpy(dest, self->f, self->Ng3_pad * sizeof(double));
+    else
+        FG_API(device_to_host(g, dest, false), "fft_exportf()");
+    return dest;
+}
+
+extern "C" void fft_importf(fft_t *self, double *src) {
+    Grid *g = G(self);
+    if (src == NULL) {
+        set_error(ERR_ARG, "src is NULL");
+        die("fft_importf()");
+    }
+    if (g->view == FFTGAL_VIEW_SYNC) {
+        memcpy(self->f, src, self->Ng3_pad * sizeof(double));
+        ++g->version;
+    } else {
+        FG_API(host_to_device(g, src, false), "fft_importf()");
+    }
+}
+
+// PCS readout (src/fft.c:134-169)
+namespace fg {
+template <typename T>
+__global__ void g2p_kernel(const T *__restrict__ f, int Ng, int Ng_pad, double Hinv, double o0, double o1,
+                           double o2, const double *__restrict__ x, const double *__restrict__ y,
+                           const double *__restrict__ z, long Np, int sum, double *__restrict__ out) {
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
+        const double pos[3] = {x[p], y[p], z[p]};
+        const double off[3] = {o0, o1, o2};
+        int c[3][4];
+        double w[3][4];
+        for (int a = 0; a < 3; ++a) {
+            const double u = __dsub_rn(__dmul_rn(pos[a], Hinv), off[a]);
+            int g1 = (int)floor(u);
+            const double d = __dsub_rn(u, (double)g1);
+            g1 = (g1 % Ng + Ng) % Ng;
+            c[a][0] = (g1 - 1 + Ng) % Ng;
+            c[a][1] = g1;
+            c[a][2] = (g1 + 1) % Ng;
+            c[a][3] = (g1 + 2) % Ng;
+            const double e = __dsub_rn(1.0, d), d2 = __dmul_rn(d, d);
+            w[a][0] = __ddiv_rn(__dmul_rn(__dmul_rn(e, e), e), 6.0);
+            w[a][1] = __ddiv_rn(__dadd_rn(__dmul_rn(__dsub_rn(__dmul_rn(3.0, d), 6.0), d2), 4.0), 6.0);
+            w[a][2] = __ddiv_rn(
+                __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(-3.0, d), 3.0), d), 3.0), d), 1.0), 6.0);
+            w[a][3] = __ddiv_rn(__dmul_rn(d2, d), 6.0);
+        }
+        double acc = 0;
+        if (sum) {
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j)
+                    for (int k = 0; k < 4; ++k)
+                        acc += (double)f[((long)c[0][i] * Ng + c[1][j]) * Ng_pad + c[2][k]] * w[0][i] * w[1][j] *
+                               w[2][k];
+        } else {
+            // the reference assigns each term, so the last one remains
+            acc = __dmul_rn(__dmul_rn(__dmul_rn((double)f[((long)c[0][3] * Ng + c[1][3]) * Ng_pad + c[2][3]],
+                                                w[0][3]),
+                                      w[1][3]),
+                            w[2][3]);
+        }
+        out[p] = acc;
+    }
+}
+
+static int g2p_run(fft_t *self, const gal_t *pos, int sum, double *host_out) {
+    Grid *g = G(self);
+    const long Np = pos->Np;
+    if (Np <= 0) return OK;
+    double *d = nullptr;
+    FG_CUDA(cudaMalloc(&d, sizeof(double) * 4 * Np));
+    cudaError_t e = cudaSuccess;
+    for (int a = 0; a < 3 && e == cudaSuccess; ++a)
+        e = cudaMemcpyAsync(d + a * Np, a == 0 ? pos->x : a == 1 ? pos->y : pos->z, sizeof(double) * Np,
+                            cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) {
+        long nb = ceil_div(Np, 256);
+        if (nb > 64L * num_sms()) nb = 64L * num_sms();
+        const double Hinv = self->Ng / self->L;
+        if (g->prec == 4)
+            g2p_kernel<float><<<(unsigned)nb, 256, 0, g->stream>>>((const float *)g->d_f, self->Ng, self->Ng_pad, Hinv,
+                                                                   self->offset[0], self->offset[1], self->offset[2],
+                                                                   d, d + Np, d + 2 * Np, Np, sum, d + 3 * Np);
+        else
+            g2p_kernel<double><<<(unsigned)nb, 256, 0, g->stream>>>((const double *)g->d_f, self->Ng, self->Ng_pad,
+                                                                    Hinv, self->offset[0], self->offset[1],
+                                                                    self->offset[2], d, d + Np, d + 2 * Np, Np, sum,
+                                                                    d + 3 * Np);
+        note_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host_out, d + 3 * Np, sizeof(double) * Np, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(d);
+    return cuda_check(e, "g2p");
+}
+}  // namespace fg
+
+extern "C" double *fft_g2p(fft_t *self, gal_t *pos) {
+    const double t = now_s();
+    Grid *g = G(self);
+    double *out = (double *)malloc((pos->Np > 0 ? pos->Np : 1) * sizeof(double));
+    if (!out) die("fft_g2p()");
+    FG_API(enter(self, true), "fft_g2p()");
+    FG_API(g2p_run(self, pos, 0, out), "fft_g2p()");
+    if (!g->quiet) fprintf(stderr, "fft_g2p() %.2fs\n", now_s() - t);
+    return out;
+}
+
+// ======================================================================================
+// reference API: src/power.h
+// ======================================================================================
+
+extern "C" void P(fft_t *grid, gal_t *part) {
+    const double t = now_s();
+    Grid *g = G(grid);
+    FG_API(enter(grid, true), "P()");
+    const double Vinv = 1 / part->V;
+    const double alpha = (part->rand == NULL) ? 0 : (double)part->Np / part->rand->Np;
+    const double Pshot = (1 + alpha) * part->V / part->Np;
+    FG_API(power_inplace(g->d_f, grid->Ng, g->prec, Vinv, Pshot, g->stream), "P()");
+    FG_API(leave(grid, true), "P()");
+    if (!g->quiet) fprintf(stderr, "P() %.2fs\n", now_s() - t);
+}
+
+namespace fg {
+// one binning pass for (los, dK, Nmu); fills the multipole and wedge sums and
+// caches the wedge sums for a following Pmu on the same grid version
+static int bin_pass(fft_t *grid, const double los_hat[3], double dK, int Nmu, BinGeometry **geo_out,
+                    std::vector<double> &Psum, std::vector<double> &Pw, int mode, double Vinv, double Pshot,
+                    cudaEvent_t *ev_end = nullptr) {
+    Grid *g = G(grid);
+    BinSpec s;
+    FG_TRY(bin_spec_init(&s, grid->Ng, grid->L, dK, los_hat, Nmu));
+    BinGeometry *geo = geometry(g, s);
+    if (!geo) return t_status ? t_status : ERR_CUDA;
+    if (geo->bad)
+        return set_error(ERR_RANGE, "a mode falls beyond the last of NK=%d k bins (dK too small for Ng)", s.NK);
+    Psum.assign((size_t)s.NK * 4, 0.0);
+    Pw.assign((size_t)s.NK * (Nmu + 1), 0.0);
+    FG_TRY(bin_power(geo, g->d_f, g->prec, mode, Vinv, Pshot, Psum.data(), Pw.data(), g->stream, ev_end));
+    *geo_out = geo;
+    return OK;
+}
+
+static void write_header(FILE *fp, int NK, double dK, const char *nlab, int nval, const fft_t *grid,
+                         const gal_t *part, double alpha, const double los[3]) {
+    fprintf(fp, "# NK %d\n", NK);
+    fprintf(fp, "# dK %g\n", dK);
+    fprintf(fp, "# %s %d\n", nlab, nval);
+    fprintf(fp, "# Ng %d\n", grid->Ng);
+    fprintf(fp, "# L %g\n", grid->L);
+    fprintf(fp, "# Np %ld\n", part->Np);
+    fprintf(fp, "# V %g\n", part->V);
+    fprintf(fp, "# alpha %g\n", alpha);
+    fprintf(fp, "# los[3] %g %g %g\n", los[0], los[1], los[2]);
+}
+
+// normalise multipole sums like src/power.c:69-76
+static int finish_pl(const BinGeometry *geo, const std::vector<double> &Psum, double *K, long *N, double *P) {
+    const BinSpec &s = geo->spec;
+    long Ntot = 0;
+    for (int b = 0; b < s.NK; ++b) {
+        const long n = geo->N[b];
+        if (K) K[b] = geo->K[b] * (s.KF / n);
+        if (N) N[b] = n;
+        if (P)
+            for (int l = 0; l < 4; ++l) P[b * 4 + l] = Psum[(size_t)b * 4 + l] * ((4 * l + 1.0) / n);
+        Ntot += n;
+    }
+    const long Ng = s.Ng;
+    if (Ntot != Ng * Ng * Ng - 1) return set_error(ERR_RANGE, "mode count %ld != Ng^3-1", Ntot);
+    return OK;
+}
+
+// merge the mu = 1 slot and normalise like src/power.c:139-153
+static int finish_pmu(const BinGeometry *geo, const std::vector<double> &Pw, double *K, long *N, double *P) {
+    const BinSpec &s = geo->spec;
+    const int Nmu = s.Nmu, W = Nmu + 1;
+    long Ntot = 0;
+    for (int b = 0; b < s.NK; ++b) {
+        std::vector<double> kk(W), pp(W);
+        std::vector<long> nn(W);
+        for (int m = 0; m < W; ++m) {
+            kk[m] = geo->Kw[(size_t)b * W + m];
+            nn[m] = geo->Nw[(size_t)b * W + m];
+            pp[m] = Pw[(size_t)b * W + m];
+        }
+        kk[Nmu - 1] += kk[Nmu];
+        nn[Nmu - 1] += nn[Nmu];
+        pp[Nmu - 1] += pp[Nmu];
+        for (int m = 0; m < Nmu; ++m) {
+            double kv = kk[m], pv = pp[m];
+            if (nn[m]) {
+                kv *= s.KF / nn[m];
+                pv /= nn[m];
+                Ntot += nn[m];
+            }
+            if (K) K[b * Nmu + m] = kv;
+            if (N) N[b * Nmu + m] = nn[m];
+            if (P) P[b * Nmu + m] = pv;
+        }
+    }
+    const long Ng = s.Ng;
+    if (Ntot != Ng * Ng * Ng - 1) return set_error(ERR_RANGE, "mode count %ld != Ng^3-1", Ntot);
+    return OK;
+}
+}  // namespace fg
+
+extern "C" void Pl(fft_t *grid, gal_t *part, double los[3], double dK, char *file) {
+    const double t = now_s();
+    Grid *g = G(grid);
+    FG_API(enter(grid, true), "Pl()");
+    hat(los);
+    const int Nmu = 3;
+    BinGeometry *geo = nullptr;
+    std::vector<double> Psum, Pw;
+    FG_API(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, 0, 0, 0), "Pl()");
+    g->wedge_cache.version = g->version;
+    g->wedge_cache.spec = geo->spec;
+    g->wedge_cache.Pw = Pw;
+    const int NK = geo->spec.NK, Nl = 4;
+    std::vector<double> K(NK), Pv((size_t)NK * Nl);
+    std::vector<long> N(NK);
+    FG_API(finish_pl(geo, Psum, K.data(), N.data(), Pv.data()), "Pl()");
+    const double alpha = (part->rand == NULL) ? 0 : (double)part->Np / part->rand->Np;
+    FILE *fp = fopen(file, "w");
+    if (!fp) {
+        set_error(ERR_ARG, "cannot open %s", file);
+        die("Pl()");
+    }
+    write_header(fp, NK, dK, "Nl", Nl, grid, part, alpha, los);
+    fprintf(fp, "# K N");
+    for (int il = 0; il < Nl; ++il) fprintf(fp, " P%d", 2 * il);
+    fprintf(fp, "\n");
+    for (int iK = 0; iK < NK; ++iK) {
+        fprintf(fp, "%e %9ld", K[iK], N[iK]);
+        for (int il = 0; il < Nl; ++il) fprintf(fp, " % e", Pv[(size_t)iK * Nl + il]);
+        fprintf(fp, "\n");
+    }
+    fclose(fp);
+    FG_API(leave(grid, false), "Pl()");
+    if (!g->quiet) fprintf(stderr, "Pl() %.2fs, saved to %s\n", now_s() - t, file);
+}
+
+extern "C" void Pmu(fft_t *grid, gal_t *part, double los[3], double dK, char *file) {
+    const double t = now_s();
+    Grid *g = G(grid);
+    hat(los);
+    const int Nmu = 3;
+    BinSpec s;
+    FG_API(bin_spec_init(&s, grid->Ng, grid->L, dK, los, Nmu), "Pmu()");
+    std::vector<double> Pw;
+    BinGeometry *geo = nullptr;
+    const auto &wc = g->wedge_cache;
+    const bool reuse = g->view == FFTGAL_VIEW_LAZY && wc.version == g->version && wc.spec.dK == s.dK &&
+                       wc.spec.L == s.L && wc.spec.Nmu == Nmu && wc.spec.los[0] == s.los[0] &&
+                       wc.spec.los[1] == s.los[1] && wc.spec.los[2] == s.los[2];
+    if (reuse) {
+        geo = geometry(g, s);
+        if (!geo) die("Pmu()");
+        Pw = wc.Pw;
+    } else {
+        FG_API(enter(grid, true), "Pmu()");
+        std::vector<double> Psum;
+        FG_API(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, 0, 0, 0), "Pmu()");
+    }
+    const int NK = s.NK;
+    std::vector<double> K((size_t)NK * Nmu), Pv((size_t)NK * Nmu);
+    std::vector<long> N((size_t)NK * Nmu);
+    FG_API(finish_pmu(geo, Pw, K.data(), N.data(), Pv.data()), "Pmu()");
+    const double alpha = (part->rand == NULL) ? 0 : (double)part->Np / part->rand->Np;
+    FILE *fp = fopen(file, "w");
+    if (!fp) {
+        set_error(ERR_ARG, "cannot open %s", file);
+        die("Pmu()");
+    }
+    write_header(fp, NK, dK, "Nmu", Nmu, grid, part, alpha, los);
+    fprintf(fp, "#");
+    for (int imu = 0; imu < Nmu; ++imu) fprintf(fp, " K%d N%d P%d", imu, imu, imu);
+    fprintf(fp, "\n");
+    for (int iK = 0; iK < NK; ++iK) {
+        fprintf(fp, "%e %9ld % e", K[(size_t)iK * Nmu], N[(size_t)iK * Nmu], Pv[(size_t)iK * Nmu]);
+        for (int imu = 1; imu < Nmu; ++imu)
+            fprintf(fp, " %e %9ld % e", K[(size_t)iK * Nmu + imu], N[(size_t)iK * Nmu + imu],
+                    Pv[(size_t)iK * Nmu + imu]);
+        fprintf(fp, "\n");
+    }
+    fclose(fp);
+    FG_API(leave(grid, false), "Pmu()");
+    if (!g->quiet) fprintf(stderr, "Pmu() %.2fs, saved to %s\n", now_s() - t, file);
+}
+
+// ======================================================================================
+// extensions: include/fftgal_gb300.h
+// ======================================================================================
+
+extern "C" int fftgal_version(void) { return 100; }
+extern "C" int fftgal_last_status(void) { return t_status; }
+extern "C" const char *fftgal_last_error(void) { return t_msg; }
+
+extern "C" int fftgal_grid_precision(const fft_t *grid) { return grid ? G(grid)->prec : 0; }
+
+extern "C" int fftgal_set_host_view(fft_t *grid, int mode) {
+    if (!grid || (mode != FFTGAL_VIEW_SYNC && mode != FFTGAL_VIEW_LAZY))
+        return set_error(ERR_ARG, "bad host-view mode");
+    Grid *g = G(grid);
+    if (g->view == FFTGAL_VIEW_LAZY && mode == FFTGAL_VIEW_SYNC) FG_TRY(device_to_host(g, grid->f, g->pinned));
+    g->view = mode;
+    return OK;
+}
+
+extern "C" int fftgal_sync_host(fft_t *grid) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    return device_to_host(G(grid), grid->f, G(grid)->pinned);
+}
+
+extern "C" int fftgal_sync_device(fft_t *grid) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    return host_to_device(G(grid), grid->f, G(grid)->pinned);
+}
+
+extern "C" int fftgal_set_stream(fft_t *grid, void *stream) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+    return OK;
+}
+
+extern "C" void *fftgal_get_stream(fft_t *grid) { return grid ? (void *)G(grid)->stream : nullptr; }
+
+extern "C" int fftgal_set_quiet(fft_t *grid, int quiet) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    G(grid)->quiet = quiet;
+    return OK;
+}
+
+extern "C" void *fftgal_device_grid(fft_t *grid) { return grid ? G(grid)->d_f : nullptr; }
+
+extern "C" int fftgal_synchronize(fft_t *grid) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    FG_CUDA(cudaStreamSynchronize(G(grid)->stream));
+    return OK;
+}
+
+extern "C" int fftgal_nk(int Ng, double L, double dK) {
+    BinSpec s;
+    const double los[3] = {0, 0, 0};
+    if (bin_spec_init(&s, Ng, L, dK, los, 1) != OK) return t_status;
+    return s.NK;
+}
+
+extern "C" int fftgal_set_timing(fft_t *grid, int on) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    if (on && !g->ev[0])
+        for (auto &e : g->ev) FG_CUDA(cudaEventCreate(&e));
+    g->timing = on;
+    return OK;
+}
+
+extern "C" int fftgal_stage_times(fft_t *grid, double out[FFTGAL_NSTAGES]) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    for (int q = 0; q <= kStages; ++q) out[q] = G(grid)->stage_ms[q];
+    return OK;
+}
+
+extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np, double V,
+                                int where, const double los_in[3], double dK, int Nmu, double *K, long *N,
+                                double *Plout, double *Kmu, long *Nmu_count, double *Pmuout) {
+    if (!grid || !x || !y || !z || Np <= 0 || !(V > 0)) return set_error(ERR_ARG, "fftgal_power_f32: bad arguments");
+    Grid *g = G(grid);
+    if (g->prec != 4) return set_error(ERR_STATE, "fftgal_power_f32 needs an FP32 grid");
+    FG_TRY(ensure_aux(g));
+    FG_TRY(ensure_tables(g));
+    const bool tm = g->timing != 0;
+    cudaStream_t st = g->stream;
+    cudaEvent_t *ev = g->ev;
+    if (tm) FG_CUDA(cudaEventRecord(ev[0], st));
+    const float *px = x, *py = y, *pz = z;
+    if (where == FFTGAL_MEM_HOST) {
+        const size_t need = (size_t)3 * Np * sizeof(float);
+        if (need > g->pos_cap) {
+            cudaFree(g->d_pos);
+            g->d_pos = nullptr;
+            FG_CUDA(cudaMalloc(&g->d_pos, need));
+            g->pos_cap = need;
+        }
+        float *d = (float *)g->d_pos;
+        FG_CUDA(cudaMemcpyAsync(d, x, sizeof(float) * Np, cudaMemcpyHostToDevice, st));
+        FG_CUDA(cudaMemcpyAsync(d + Np, y, sizeof(float) * Np, cudaMemcpyHostToDevice, st));
+        FG_CUDA(cudaMemcpyAsync(d + 2 * Np, z, sizeof(float) * Np, cudaMemcpyHostToDevice, st));
+        px = d;
+        py = d + Np;
+        pz = d + 2 * Np;
+    }
+    if (tm) FG_CUDA(cudaEventRecord(ev[1], st));
+    const int Ng = grid->Ng;
+    const double Hinv = Ng / grid->L;
+    const double H3 = H3_of(g);
+    const double nbar = Np / V;
+    const double Npcinv = 1 / nbar / H3;
+    PaintGridSpec spec[2];
+    spec[0].out = g->d_f;
+    spec[1].out = g->d_aux;
+    for (int a = 0; a < 3; ++a) {
+        spec[0].offset[a] = 0;
+        spec[1].offset[a] = remainder(0.5, Ng);
+    }
+    spec[0].scale = spec[1].scale = Npcinv;
+    FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, 2, st, tm ? ev + 2 : nullptr));
+    void *grids[2] = {g->d_f, g->d_aux};
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
+    if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
+    FG_TRY(fft_pass_j(&g->fft, grids, 2, -1, st));
+    if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
+    FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
+    if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
+    FG_TRY(scale_grid(g->d_aux, grid->Ng3_pad, 4, H3, st));
+    FG_TRY(phase(g, g->d_aux, spec[1].offset, 1));
+    FG_TRY(scale_grid(g->d_f, grid->Ng3_pad, 4, H3, st));
+    FG_TRY(interlace_average(g->d_f, g->d_aux, grid->Ng3_pad, 4, st));
+    FG_TRY(deconv(g, g->d_f));
+    if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
+    for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
+    ++g->version;
+    double los[3] = {los_in[0], los_in[1], los_in[2]};
+    hat(los);
+    BinGeometry *geo = nullptr;
+    std::vector<double> Psum, Pw;
+    const double Vinv = 1 / V;
+    const double Pshot = V / Np;
+    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, 1, Vinv, Pshot, tm ? &ev[10] : nullptr));
+    if (tm) {
+        FG_CUDA(cudaEventSynchronize(ev[kStages]));
+        float ms;
+        for (int q = 0; q < kStages; ++q) {
+            FG_CUDA(cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
+            g->stage_ms[q] = ms;
+        }
+        FG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[kStages]));
+        g->stage_ms[kStages] = ms;
+    }
+    FG_TRY(finish_pl(geo, Psum, K, N, Plout));
+    FG_TRY(finish_pmu(geo, Pw, Kmu, Nmu_count, Pmuout));
+    if (g->view == FFTGAL_VIEW_SYNC) FG_TRY(device_to_host(g, grid->f, g->pinned));
+    return OK;
+}
+
+extern "C" int fftgal_g2p_sum(fft_t *grid, const gal_t *pos, double *out) {
+    if (!grid || !pos || !out) return set_error(ERR_ARG, "null argument");
+    FG_TRY(enter(grid, true));
+    return g2p_run(grid, pos, 1, out);
+}
+
+extern "C" long fftgal_launch_count(void) { return launch_count(); }
+
+extern "C" long fftgal_device_bytes(fft_t *grid) {
+    if (!grid) return 0;
+    Grid *g = G(grid);
+    long b = (long)g->prec * g->Ng3_pad * (g->d_aux ? 2 : 1);
+    b += (long)g->pos_cap + (long)g->stage_cap + (long)g->scratch.bytes;
+    return b;
+}

@@ -1,0 +1,384 @@
+// k-shell binning of the half spectrum for sm_103a: multipoles l = 0,2,4,6
+// (src/power.c:30-101) and mu wedges (src/power.c:104-178) in one pass.
+//
+// Mode classification is exact with respect to the reference's FP64 code:
+//  * the k bin iK = floor(sqrt(n2) * dKinv) depends only on the integer
+//    n2 = kx^2 + ky^2 + kz^2, so the host evaluates the reference expression
+//    once per n2 and ships the bin thresholds; the kernel finds iK from an FP32
+//    estimate corrected against those exact thresholds;
+//  * the wedge imu = floor(|mu * Nmu|) is estimated in FP32 and, only when the
+//    estimate lies within its error bound of a wedge edge, re-evaluated in FP64
+//    with the reference's operation order (explicitly rounded, no FMA).
+// Mode counts N and the mean |k| per bin do not depend on the data: they are
+// built once per (Ng, L, dK, los, Nmu) from an exact (n2, imu) multiplicity
+// histogram and cached; every catalog then only accumulates power sums.
+// Power sums: per-warp segmented reductions over runs of equal bins, FP32
+// shared-memory accumulators flushed every chunk of rows into FP64 shared
+// accumulators, FP64 global atomics once per CTA.
+#include "internal.h"
+#include "common.cuh"
+
+#include <math.h>
+#include <string.h>
+#include <vector>
+
+namespace fg {
+
+constexpr double kSqrt3 = 1.73205080756887729352744634151;
+
+int bin_spec_init(BinSpec *b, int Ng, double L, double dK, const double los_hat[3], int Nmu) {
+    if (!(dK > 0) || !(L > 0)) return set_error(ERR_ARG, "dK and L must be > 0");
+    if (Nmu < 1 || Nmu > 64) return set_error(ERR_ARG, "Nmu must be in [1, 64]");
+    b->Ng = Ng;
+    b->L = L;
+    b->dK = dK;
+    for (int a = 0; a < 3; ++a) b->los[a] = los_hat[a];
+    b->Nmu = Nmu;
+    b->KF = 2 * M_PI / L;
+    b->dKinv = b->KF / dK;
+    // src/power.c:34-36
+    b->NK = (int)floor(kSqrt3 * (Ng / 2) * b->dKinv) + 1;
+    if (b->NK < 1 || b->NK > (1 << 20)) return set_error(ERR_ARG, "NK = %d out of range", b->NK);
+    return OK;
+}
+
+struct BinDev {
+    int Ng, nh, NK, Nmu, W;     // W = Nmu + 1 wedge slots
+    float dKinv_f;
+    double l0, l1, l2;
+    float l0f, l1f, l2f;
+    bool zero_los;
+};
+
+// signed wavenumber index of grid index i: the reference's Kval table
+// (src/power.c:46-51), where the even-Ng Nyquist entry ends up as -Ng/2
+__device__ __forceinline__ int kval(int i, int Ng) { return 2 * i < Ng ? i : i - Ng; }
+
+__device__ __forceinline__ int kbin(uint32_t n2, const uint32_t *thr, int NK, float dKinv_f) {
+    int b = (int)(sqrtf((float)n2) * dKinv_f);
+    b = b < 0 ? 0 : (b > NK ? NK : b);
+    while (b > 0 && n2 < thr[b]) --b;
+    while (b < NK && n2 >= thr[b + 1]) ++b;
+    return b;  // == NK means beyond the last bin
+}
+
+// exact wedge index, reference expression (src/power.c:131-134)
+__device__ __forceinline__ int wedge_exact(int ki, int kj, int kk, const BinDev &d) {
+    const double a = (double)ki, b = (double)kj, c = (double)kk;
+    const double kamp = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)));
+    const double num = __dadd_rn(__dadd_rn(__dmul_rn(a, d.l0), __dmul_rn(b, d.l1)), __dmul_rn(c, d.l2));
+    const double mu = __ddiv_rn(num, kamp);
+    return (int)floor(fabs(__dmul_rn(mu, (double)d.Nmu)));
+}
+
+// wedge index and mu^2 (FP32) for one mode
+__device__ __forceinline__ int wedge_index(int ki, int kj, int kk, float kamp, const BinDev &d,
+                                           float &mu2) {
+    if (d.zero_los) {
+        mu2 = 0.f;
+        return 0;
+    }
+    const float num = (float)ki * d.l0f + (float)kj * d.l1f + (float)kk * d.l2f;
+    const float mu = num / kamp;
+    mu2 = mu * mu;
+    const float t = fabsf(mu * (float)d.Nmu);
+    const float eps = 2e-6f * (float)(d.Nmu + 1);
+    const float r = rintf(t);
+    if (r >= 1.f && fabsf(t - r) < eps) return wedge_exact(ki, kj, kk, d);
+    return (int)t;
+}
+
+// ---- geometry: exact (n2, imu) multiplicities -----------------------------------------------
+__global__ void geometry_kernel(BinDev d, uint32_t *__restrict__ hist) {
+    const long n = (long)d.Ng * d.Ng * d.nh;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        if (e == 0) continue;  // the k = 0 mode is skipped (src/power.c:52-54)
+        const int k = (int)(e % d.nh);
+        const long row = e / d.nh;
+        const int j = (int)(row % d.Ng), i = (int)(row / d.Ng);
+        const int ki = kval(i, d.Ng), kj = kval(j, d.Ng), kk = kval(k, d.Ng);
+        const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
+        const uint32_t count = 1 + ((2 * k) % d.Ng > 0);
+        float mu2;
+        const int imu = wedge_index(ki, kj, kk, sqrtf((float)n2), d, mu2);
+        atomicAdd(&hist[(size_t)n2 * d.W + imu], count);
+    }
+}
+
+static BinDev make_dev(const BinSpec &s) {
+    BinDev d;
+    d.Ng = s.Ng;
+    d.nh = s.Ng / 2 + 1;
+    d.NK = s.NK;
+    d.Nmu = s.Nmu;
+    d.W = s.Nmu + 1;
+    d.dKinv_f = (float)s.dKinv;
+    d.l0 = s.los[0];
+    d.l1 = s.los[1];
+    d.l2 = s.los[2];
+    d.l0f = (float)s.los[0];
+    d.l1f = (float)s.los[1];
+    d.l2f = (float)s.los[2];
+    d.zero_los = (s.los[0] == 0 && s.los[1] == 0 && s.los[2] == 0);
+    return d;
+}
+
+void bin_geometry_free(BinGeometry *g) {
+    delete[] g->N;
+    delete[] g->K;
+    delete[] g->Nw;
+    delete[] g->Kw;
+    cudaFree(g->d_thr);
+    cudaFree(g->d_acc);
+    *g = BinGeometry();
+}
+
+int bin_geometry_build(BinGeometry *g, const BinSpec &s, cudaStream_t st) {
+    bin_geometry_free(g);
+    g->spec = s;
+    const int Ng = s.Ng, NK = s.NK, W = s.Nmu + 1;
+    const int h = Ng / 2;
+    const uint32_t n2max = (uint32_t)(3L * h * h);
+    // exact k-bin thresholds from the reference expression floor(sqrt(n2) * dKinv)
+    std::vector<uint32_t> thr(NK + 2, n2max + 1);
+    std::vector<int> ik(n2max + 1);
+    for (uint32_t n2 = 0; n2 <= n2max; ++n2) {
+        volatile double kamp = sqrt((double)n2);
+        volatile double t = kamp * s.dKinv;
+        ik[n2] = (int)floor(t);
+    }
+    thr[0] = 0;
+    {
+        int b = 1;
+        for (uint32_t n2 = 0; n2 <= n2max && b <= NK; ++n2)
+            while (b <= NK && ik[n2] >= b) thr[b++] = n2;
+    }
+    FG_CUDA(cudaMalloc(&g->d_thr, sizeof(uint32_t) * (NK + 2)));
+    FG_CUDA(cudaMemcpyAsync(g->d_thr, thr.data(), sizeof(uint32_t) * (NK + 2), cudaMemcpyHostToDevice, st));
+    // multiplicity histogram over (n2, imu)
+    const size_t hlen = (size_t)(n2max + 1) * W;
+    uint32_t *d_hist = nullptr;
+    FG_CUDA(cudaMalloc(&d_hist, sizeof(uint32_t) * hlen));
+    FG_CUDA(cudaMemsetAsync(d_hist, 0, sizeof(uint32_t) * hlen, st));
+    const BinDev d = make_dev(s);
+    const long nmodes = (long)Ng * Ng * (h + 1);
+    long nb = ceil_div(nmodes, 256);
+    if (nb > 64L * num_sms()) nb = 64L * num_sms();
+    geometry_kernel<<<(unsigned)nb, 256, 0, st>>>(d, d_hist);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    std::vector<uint32_t> hh(hlen);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hh.data(), d_hist, sizeof(uint32_t) * hlen, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_hist);
+    if (e != cudaSuccess) return cuda_check(e, "geometry histogram");
+    g->N = new long[NK]();
+    g->K = new double[NK]();
+    g->Nw = new long[(size_t)NK * W]();
+    g->Kw = new double[(size_t)NK * W]();
+    g->bad = 0;
+    for (uint32_t n2 = 1; n2 <= n2max; ++n2) {
+        const uint32_t *row = &hh[(size_t)n2 * W];
+        long tot = 0;
+        for (int m = 0; m < W; ++m) tot += row[m];
+        if (!tot) continue;
+        const int b = ik[n2];
+        if (b < 0 || b >= NK) {
+            g->bad = 1;
+            continue;
+        }
+        const double kamp = sqrt((double)n2);
+        g->N[b] += tot;
+        g->K[b] += (double)tot * kamp;
+        for (int m = 0; m < W; ++m)
+            if (row[m]) {
+                g->Nw[(size_t)b * W + m] += row[m];
+                g->Kw[(size_t)b * W + m] += (double)row[m] * kamp;
+            }
+    }
+    g->acc_len = (size_t)NK * (4 + W);
+    FG_CUDA(cudaMalloc(&g->d_acc, sizeof(double) * g->acc_len));
+    g->valid = true;
+    return OK;
+}
+
+// ---- power sums ---------------------------------------------------------------------------------
+
+constexpr int kBinThreads = 256;
+constexpr int kChunkRows = 64;
+
+// inclusive segmented sum over runs of equal `key` within the warp; returns
+// true on the last lane of each run (which then owns the run's sum)
+template <int NV>
+__device__ __forceinline__ bool warp_segsum(int key, float (&v)[NV], int lane) {
+    const unsigned full = 0xffffffffu;
+    const int kprev = __shfl_up_sync(full, key, 1);
+    const bool head = lane == 0 || kprev != key;
+    const unsigned hm = __ballot_sync(full, head);
+    const int seg = __popc(hm & (0xffffffffu >> (31 - lane)));
+    if (hm != 1u) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int sseg = __shfl_up_sync(full, seg, o);
+            float t[NV];
+#pragma unroll
+            for (int q = 0; q < NV; ++q) t[q] = __shfl_up_sync(full, v[q], o);
+            if (lane >= o && sseg == seg) {
+#pragma unroll
+                for (int q = 0; q < NV; ++q) v[q] += t[q];
+            }
+        }
+        const int snext = __shfl_down_sync(full, seg, 1);
+        return lane == 31 || snext != seg;
+    }
+    // a single run: butterfly reduction, lane 31 owns the total
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) v[q] += __shfl_xor_sync(full, v[q], o);
+    return lane == 31;
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kBinThreads)
+bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
+                 const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, int Ng_pad) {
+    using T2 = vec2_t<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int NK = d.NK, W = d.W, NQ = 4 + W;
+    double *acc64 = reinterpret_cast<double *>(smem_raw);          // [NK * NQ]
+    float *acc32 = reinterpret_cast<float *>(acc64 + (size_t)NK * NQ);  // [NK * NQ] (FP32 grids)
+    uint32_t *thr = reinterpret_cast<uint32_t *>(acc32 + (sizeof(T) == 4 ? (size_t)NK * NQ : 0));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    for (int e = tid; e < NK * NQ; e += blockDim.x) {
+        acc64[e] = 0;
+        if constexpr (sizeof(T) == 4) acc32[e] = 0.f;
+    }
+    for (int e = tid; e < NK + 2; e += blockDim.x) thr[e] = thr_g[e];
+    __syncthreads();
+
+    const long nrows = (long)d.Ng * d.Ng;
+    const long nchunks = ceil_div(nrows, kChunkRows);
+    for (long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const long e0 = ch * kChunkRows * d.nh;
+        const long e1 = min(nrows, (ch + 1) * kChunkRows) * d.nh;
+        for (long base = e0 + (long)warp * 32; base < e1; base += (long)nwarp * 32) {
+            const long e = base + lane;
+            int b = -1, imu = 0;
+            T pc = 0, mu2t = 0;
+            if (e < e1 && e > 0) {
+                const int k = (int)(e % d.nh);
+                const long row = e / d.nh;
+                const int j = (int)(row % d.Ng), i = (int)(row / d.Ng);
+                const int ki = kval(i, d.Ng), kj = kval(j, d.Ng), kk = kval(k, d.Ng);
+                const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
+                const int count = 1 + ((2 * k) % d.Ng > 0);
+                T p;
+                if constexpr (MODE == 0) {
+                    p = f[row * Ng_pad + 2 * k];
+                } else {
+                    const T2 v = reinterpret_cast<const T2 *>(f)[e];
+                    if constexpr (sizeof(T) == 8)
+                        p = __dsub_rn(__dmul_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), Vinv), Pshot);
+                    else
+                        p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+                }
+                pc = p * (T)count;
+                b = kbin(n2, thr, NK, d.dKinv_f);
+                if (b >= NK) b = -1;
+                const float kampf = sqrtf((float)n2);
+                float mu2f;
+                imu = wedge_index(ki, kj, kk, kampf, d, mu2f);
+                if constexpr (sizeof(T) == 8) {
+                    if (!d.zero_los) {
+                        const double kamp = __dsqrt_rn((double)n2);
+                        const double num = __dadd_rn(__dadd_rn(__dmul_rn((double)ki, d.l0), __dmul_rn((double)kj, d.l1)),
+                                                     __dmul_rn((double)kk, d.l2));
+                        const double mu = __ddiv_rn(num, kamp);
+                        mu2t = __dmul_rn(mu, mu);
+                    }
+                } else {
+                    mu2t = mu2f;
+                }
+            }
+            if constexpr (sizeof(T) == 8) {
+                if (b >= 0) {
+                    const double m2 = mu2t;
+                    double *a = acc64 + (size_t)b * NQ;
+                    atomicAdd(a + 0, pc);
+                    atomicAdd(a + 1, pc * (1.5 * m2 - 0.5));
+                    atomicAdd(a + 2, pc * ((4.375 * m2 - 3.75) * m2 + 0.375));
+                    atomicAdd(a + 3, pc * (((14.4375 * m2 - 19.6875) * m2 + 6.5625) * m2 - 0.3125));
+                    atomicAdd(a + 4 + imu, pc);
+                }
+            } else {
+                const float m2 = mu2t;
+                float v[4] = {pc, pc * (1.5f * m2 - 0.5f), pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f),
+                              pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f)};
+                if (warp_segsum<4>(b, v, lane) && b >= 0) {
+                    float *a = acc32 + (size_t)b * NQ;
+                    atomicAdd(a + 0, v[0]);
+                    atomicAdd(a + 1, v[1]);
+                    atomicAdd(a + 2, v[2]);
+                    atomicAdd(a + 3, v[3]);
+                }
+                float w[1] = {pc};
+                const int wkey = b < 0 ? -1 : b * W + imu;
+                if (warp_segsum<1>(wkey, w, lane) && wkey >= 0) atomicAdd(acc32 + (size_t)b * NQ + 4 + imu, w[0]);
+            }
+        }
+        if constexpr (sizeof(T) == 4) {
+            __syncthreads();
+            for (int e = tid; e < NK * NQ; e += blockDim.x) {
+                acc64[e] += (double)acc32[e];
+                acc32[e] = 0.f;
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < NK * NQ; e += blockDim.x)
+        if (acc64[e] != 0) atomicAdd(&gacc[e], acc64[e]);
+}
+
+int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
+              double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end) {
+    if (!g->valid) return set_error(ERR_STATE, "bin geometry not built");
+    const BinSpec &s = g->spec;
+    const BinDev d = make_dev(s);
+    const int NK = s.NK, W = s.Nmu + 1, NQ = 4 + W;
+    size_t smem = (size_t)NK * NQ * 8 + (prec == 4 ? (size_t)NK * NQ * 4 : 0) + sizeof(uint32_t) * (NK + 2);
+    if (smem > 220 * 1024)
+        return set_error(ERR_UNSUPPORTED, "binning: %d k bins x %d wedges exceed shared memory", NK, s.Nmu);
+    FG_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(double) * g->acc_len, st));
+    const int Ng_pad = 2 * (s.Ng / 2 + 1);
+    const long nchunks = ceil_div((long)s.Ng * s.Ng, kChunkRows);
+    int per_sm = smem > 110 * 1024 ? 1 : 2;
+    long nb = (long)num_sms() * per_sm;
+    if (nb > nchunks) nb = nchunks;
+#define FG_BIN_LAUNCH(T, M)                                                                            \
+    do {                                                                                               \
+        FG_CUDA(cudaFuncSetAttribute(bin_power_kernel<T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                                      \
+        bin_power_kernel<T, M><<<(unsigned)nb, kBinThreads, smem, st>>>(                               \
+            d, (const T *)f, (T)Vinv, (T)Pshot, g->d_thr, g->d_acc, Ng_pad);                           \
+    } while (0)
+    if (prec == 4) {
+        if (mode == 0) FG_BIN_LAUNCH(float, 0); else FG_BIN_LAUNCH(float, 1);
+    } else {
+        if (mode == 0) FG_BIN_LAUNCH(double, 0); else FG_BIN_LAUNCH(double, 1);
+    }
+#undef FG_BIN_LAUNCH
+    FG_LAUNCHED(1);
+    if (ev_end) FG_CUDA(cudaEventRecord(*ev_end, st));
+    std::vector<double> h(g->acc_len);
+    FG_CUDA(cudaMemcpyAsync(h.data(), g->d_acc, sizeof(double) * g->acc_len, cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    for (int b = 0; b < NK; ++b) {
+        for (int l = 0; l < 4; ++l) Psum[b * 4 + l] = h[(size_t)b * NQ + l];
+        for (int m = 0; m < W; ++m) Pw[(size_t)b * W + m] = h[(size_t)b * NQ + 4 + m];
+    }
+    return OK;
+}
+
+}  // namespace fg

@@ -1,0 +1,177 @@
+// Internal declarations shared by the CUDA translation units of
+// libfftgal_gb300.so.  Nothing here is part of the public C ABI
+// (include/fft.h, include/power.h, include/gal.h, include/fftgal_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+namespace fg {
+
+// ---- status / errors ------------------------------------------------------
+enum Status {
+    OK = 0,
+    ERR_ARG = -1,
+    ERR_CUDA = -2,
+    ERR_NOMEM = -3,
+    ERR_UNSUPPORTED = -4,
+    ERR_RANGE = -5,
+    ERR_STATE = -6,
+};
+
+// records a status with a message (thread-local); returns the status
+int set_error(int status, const char *fmt, ...);
+int cuda_check(cudaError_t e, const char *what);
+
+#define FG_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t fg_e_ = (call);                                     \
+        if (fg_e_ != cudaSuccess) return ::fg::cuda_check(fg_e_, #call); \
+    } while (0)
+
+// every kernel launch site reports here (counted for the benchmark's
+// launch tally) and checks the launch
+void note_launches(int n);
+long launch_count();
+#define FG_LAUNCHED(n)                                                      \
+    do {                                                                    \
+        ::fg::note_launches(n);                                             \
+        cudaError_t fg_e_ = cudaGetLastError();                             \
+        if (fg_e_ != cudaSuccess) return ::fg::cuda_check(fg_e_, "launch"); \
+    } while (0)
+
+#define FG_TRY(expr)                  \
+    do {                              \
+        int fg_s_ = (expr);           \
+        if (fg_s_ != 0) return fg_s_; \
+    } while (0)
+
+// ---- FFT plans -------------------------------------------------------------
+constexpr int kMaxRadixPasses = 16;
+
+struct Fft1dPlan {
+    int n = 0;                    // complex length
+    int nrad = 0;
+    int rad[kMaxRadixPasses] = {};
+    void *tw = nullptr;           // device: exp(-2 pi i t / n), t < n (float2 or double2)
+};
+
+struct FftPlan {
+    int prec = 4;                 // 4 = float, 8 = double
+    int Ng = 0, nh = 0;
+    bool even = true;
+    Fft1dPlan axis;               // length Ng (j and i axes; odd-Ng k axis)
+    Fft1dPlan half;               // length Ng/2 (k axis, even Ng)
+    void *rtw = nullptr;          // device: exp(-2 pi i k / Ng), k <= Ng/2 (r2c split)
+    // launch shapes chosen by the planner
+    int cols = 16, col_threads = 256;      // column kernel: columns per CTA
+    int rows = 16, row_threads = 256;      // k-axis kernel: rows per CTA
+    size_t col_smem = 0, row_smem = 0;
+};
+
+int fft_plan_create(FftPlan *p, int Ng, int prec);
+void fft_plan_destroy(FftPlan *p);
+// forward r2c (sign -1) of `ngrids` in-place padded grids, unnormalised
+int fft_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
+// backward c2r (sign +1), unnormalised
+int fft_c2r(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
+// the three passes separately (used by the fused pipeline)
+int fft_pass_k_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
+int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
+int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
+// i-axis pass of two grids fused with the interlacing finish:
+// A <- scale * 0.5 * (A + B * phaseB) * Winv3   (see spectral tables)
+int fft_pass_i_interlace(const FftPlan *p, void *gridA, void *gridB,
+                         const void *phase_tab, const void *winv_tab, double scale,
+                         cudaStream_t s);
+
+// ---- paint -----------------------------------------------------------------
+struct PaintTiling {
+    int Ng = 0;
+    int nt = 0;                   // tiles per axis
+    int tmax = 0;                 // largest tile extent
+    int *d_tables = nullptr;      // device: tile_of[Ng], start[nt+1]
+    long nkeys = 0;               // nt^3 * 27
+};
+
+struct PaintScratch {
+    long cap_particles = 0;
+    uint32_t *key = nullptr;      // [cap] tile/class key of each particle
+    uint32_t *rank = nullptr;     // [cap] rank within its key
+    void *sorted = nullptr;       // [cap] sorted records (float4 or double x3)
+    long cap_keys = 0;
+    uint32_t *hist = nullptr;     // [nkeys + 1] counts -> exclusive offsets
+    uint32_t *scan_tmp = nullptr; // block sums for the scan
+    size_t bytes = 0;
+};
+
+struct PaintGridSpec {
+    void *out = nullptr;          // padded real grid (float or double)
+    double offset[3] = {0, 0, 0}; // already reduced with remainder()
+    double scale = 1.0;           // Npcinv (times -alpha for randoms)
+    int accumulate = 0;           // 0: overwrite (and zero padding), 1: out += value
+};
+
+int paint_tiling_create(PaintTiling *t, int Ng, int tile);
+void paint_tiling_destroy(PaintTiling *t);
+void paint_scratch_free(PaintScratch *s);
+
+// Paint one catalog onto 1 or 2 grids (same tiling, offsets within 1 cell of
+// each other).  pos_prec: 4 (float x,y,z) or 8 (double x,y,z); device pointers.
+// `ev` (optional, 4 events) is recorded after the key, scan, scatter and
+// tile-paint kernels.
+int paint(const PaintTiling *t, PaintScratch *s, int grid_prec,
+          const void *x, const void *y, const void *z, int pos_prec, long Np,
+          double Hinv, const PaintGridSpec *grids, int ngrids, cudaStream_t st,
+          cudaEvent_t *ev = nullptr);
+
+// ---- spectral elementwise ----------------------------------------------------
+int scale_grid(void *f, long n, int prec, double s, cudaStream_t st);
+// offset phase with the reference's Nyquist behaviour; tab = [3][Ng] complex (double)
+int build_phase_table(double *host_tab, int Ng, const double offset[3], int onoff);
+int apply_phase(void *f, int Ng, int prec, const void *d_tab, cudaStream_t st);
+int build_winv_table(double *host_tab, int Ng);
+int apply_deconv(void *f, int Ng, int prec, const void *d_winv, cudaStream_t st);
+int interlace_average(void *f, const void *fdual, long n, int prec, cudaStream_t st);
+int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStream_t st);
+int convert_grid(void *dst, int dst_prec, const void *src, int src_prec, long n, cudaStream_t st);
+
+// ---- binning -----------------------------------------------------------------
+struct BinSpec {
+    int Ng = 0;
+    double L = 0, dK = 0;
+    double los[3] = {0, 0, 0};    // already normalised with hat()
+    int Nmu = 3;
+    int NK = 0;
+    double KF = 0, dKinv = 0;
+};
+
+struct BinGeometry {               // data-independent part, cached
+    BinSpec spec;
+    bool valid = false;
+    long *N = nullptr;            // host [NK]
+    double *K = nullptr;          // host [NK] (sum count*Kamp)
+    long *Nw = nullptr;           // host [NK][Nmu+1]
+    double *Kw = nullptr;         // host [NK][Nmu+1]
+    uint32_t *d_thr = nullptr;    // device: n2 thresholds of the k bins [NK+1]
+    double *d_acc = nullptr;      // device accumulators (per call)
+    size_t acc_len = 0;
+    int bad = 0;
+};
+
+int bin_spec_init(BinSpec *b, int Ng, double L, double dK, const double los_hat[3], int Nmu);
+int bin_geometry_build(BinGeometry *g, const BinSpec &spec, cudaStream_t st);
+void bin_geometry_free(BinGeometry *g);
+// power sums over the half spectrum.  mode 0: input holds P (F_Re = P, from P());
+// mode 1: input holds delta (complex), P = |delta|^2 * Vinv - Pshot computed on the fly.
+// Results (host): Psum[NK][4] (count-weighted, times Legendre), Pw[NK][Nmu+1].
+// `ev_end` (optional) is recorded right after the binning kernel
+int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
+              double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end = nullptr);
+
+// ---- misc -----------------------------------------------------------------------
+int num_sms();
+int device_max_smem();
+
+}  // namespace fg

@@ -1,0 +1,232 @@
+// Full-grid elementwise passes of the reference path, for sm_103a:
+//   scale            src/fft.c:128-129, 176-177, 188-189   (f *= H^3, 1/L^3, Npcinv)
+//   offset phase     src/fft.c:196-233 (with its Nyquist-table behaviour)
+//   deconvolution    src/fft.c:236-254 (PCS window sinc^-4 per axis)
+//   interlace mean   src/fft.c:270-271 (f = 0.5 (f_dual + f))
+//   power            src/power.c:12-27 (F_Re = |F|^2/V - Pshot, F_Im = 0, DC = 0)
+//   precision change (device grid <-> double host view)
+// FP64 grids evaluate every product and sum in the reference's order with
+// explicitly rounded intrinsics (no FMA contraction), so they reproduce the
+// reference's arithmetic; FP32 grids use the same formulas in FP32.
+#include "internal.h"
+#include "common.cuh"
+
+#include <math.h>
+#include <vector>
+
+namespace fg {
+
+static unsigned grid_blocks(long n, int threads) {
+    long b = ceil_div(n, threads);
+    const long cap = 64L * num_sms();
+    return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+// ---- scale -------------------------------------------------------------------
+template <typename T>
+__global__ void scale_kernel(T *f, long n, T s) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        f[e] = f[e] * s;
+}
+
+int scale_grid(void *f, long n, int prec, double s, cudaStream_t st) {
+    if (prec == 4)
+        scale_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, n, (float)s);
+    else
+        scale_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, n, s);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+// ---- offset phase ---------------------------------------------------------------
+// table: [3][Ng] complex in FP64, built exactly as src/fft.c:201-215 builds it
+int build_phase_table(double *tab, int Ng, const double offset[3], int onoff) {
+    onoff = onoff > 0 ? 1 : -1;
+    for (int a = 0; a < 3; ++a) {
+        tab[(a * Ng + 0) * 2 + 0] = 1;
+        tab[(a * Ng + 0) * 2 + 1] = 0;
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int n = 1; n <= Ng / 2; ++n) {
+            volatile double arg = -onoff * 2 * M_PI * n / Ng * offset[a];
+            const double c = cos(arg), s = sin(arg);
+            tab[(a * Ng + n) * 2 + 0] = c;
+            tab[(a * Ng + n) * 2 + 1] = s;
+            tab[(a * Ng + Ng - n) * 2 + 0] = c;
+            tab[(a * Ng + Ng - n) * 2 + 1] = -s;
+        }
+    return OK;
+}
+
+template <typename T>
+__device__ __forceinline__ void phase_of(const double *__restrict__ tab, int Ng, int i, int j, int k,
+                                         T &pr, T &pi) {
+    if constexpr (sizeof(T) == 8) {
+        const double ar = tab[2 * i], ai = tab[2 * i + 1];
+        const double br = tab[2 * (Ng + j)], bi = tab[2 * (Ng + j) + 1];
+        const double cr = tab[2 * (2 * Ng + k)], ci = tab[2 * (2 * Ng + k) + 1];
+        // src/fft.c:217-228, left to right
+        pr = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(__dmul_rn(ar, br), cr), __dmul_rn(__dmul_rn(ar, bi), ci)),
+                                 __dmul_rn(__dmul_rn(ai, br), ci)),
+                       __dmul_rn(__dmul_rn(ai, bi), cr));
+        pi = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(ai, br), cr), __dmul_rn(__dmul_rn(ar, bi), cr)),
+                                 __dmul_rn(__dmul_rn(ar, br), ci)),
+                       __dmul_rn(__dmul_rn(ai, bi), ci));
+    } else {
+        const float ar = (float)tab[2 * i], ai = (float)tab[2 * i + 1];
+        const float br = (float)tab[2 * (Ng + j)], bi = (float)tab[2 * (Ng + j) + 1];
+        const float cr = (float)tab[2 * (2 * Ng + k)], ci = (float)tab[2 * (2 * Ng + k) + 1];
+        const float xr = ar * br - ai * bi, xi = ar * bi + ai * br;
+        pr = xr * cr - xi * ci;
+        pi = xr * ci + xi * cr;
+    }
+}
+
+template <typename T>
+__global__ void phase_kernel(T *f, int Ng, const double *__restrict__ tab) {
+    using T2 = vec2_t<T>;
+    const int nh = Ng / 2 + 1;
+    const long n = (long)Ng * Ng * nh;
+    T2 *c = reinterpret_cast<T2 *>(f);
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % nh);
+        const long row = e / nh;
+        const int j = (int)(row % Ng), i = (int)(row / Ng);
+        T pr, pi;
+        phase_of<T>(tab, Ng, i, j, k, pr, pi);
+        const T2 v = c[e];
+        if constexpr (sizeof(T) == 8)
+            c[e] = mk2<T2>(__dsub_rn(__dmul_rn(v.x, pr), __dmul_rn(v.y, pi)),
+                           __dadd_rn(__dmul_rn(v.x, pi), __dmul_rn(v.y, pr)));
+        else
+            c[e] = mk2<T2>(v.x * pr - v.y * pi, v.x * pi + v.y * pr);
+    }
+}
+
+int apply_phase(void *f, int Ng, int prec, const void *d_tab, cudaStream_t st) {
+    const long n = (long)Ng * Ng * (Ng / 2 + 1);
+    if (prec == 4)
+        phase_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, (const double *)d_tab);
+    else
+        phase_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, (const double *)d_tab);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+// ---- deconvolution ------------------------------------------------------------------
+int build_winv_table(double *w, int Ng) {
+    w[0] = 1;
+    for (int n = 1; n <= Ng / 2; ++n) {
+        const double arg = M_PI * n / Ng;
+        const double r = arg / sin(arg);
+        const double r2 = r * r;
+        w[n] = r2 * r2;
+        w[Ng - n] = w[n];
+    }
+    return OK;
+}
+
+template <typename T>
+__global__ void deconv_kernel(T *f, int Ng, const double *__restrict__ winv) {
+    using T2 = vec2_t<T>;
+    const int nh = Ng / 2 + 1;
+    const long n = (long)Ng * Ng * nh;
+    T2 *c = reinterpret_cast<T2 *>(f);
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % nh);
+        const long row = e / nh;
+        const int j = (int)(row % Ng), i = (int)(row / Ng);
+        const T2 v = c[e];
+        if constexpr (sizeof(T) == 8) {
+            const double w3 = __dmul_rn(__dmul_rn(winv[i], winv[j]), winv[k]);
+            c[e] = mk2<T2>(__dmul_rn(v.x, w3), __dmul_rn(v.y, w3));
+        } else {
+            const float w3 = (float)(winv[i] * winv[j] * winv[k]);
+            c[e] = mk2<T2>(v.x * w3, v.y * w3);
+        }
+    }
+}
+
+int apply_deconv(void *f, int Ng, int prec, const void *d_winv, cudaStream_t st) {
+    const long n = (long)Ng * Ng * (Ng / 2 + 1);
+    if (prec == 4)
+        deconv_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, (const double *)d_winv);
+    else
+        deconv_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, (const double *)d_winv);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+// ---- interlacing average --------------------------------------------------------------
+template <typename T>
+__global__ void average_kernel(T *f, const T *__restrict__ g, long n) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        if constexpr (sizeof(T) == 8)
+            f[e] = __dmul_rn(0.5, __dadd_rn(g[e], f[e]));
+        else
+            f[e] = 0.5f * (g[e] + f[e]);
+    }
+}
+
+int interlace_average(void *f, const void *fdual, long n, int prec, cudaStream_t st) {
+    if (prec == 4)
+        average_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, (const float *)fdual, n);
+    else
+        average_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, (const double *)fdual, n);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+// ---- P(): |delta|^2 / V - Pshot in place ---------------------------------------------------
+template <typename T>
+__global__ void power_kernel(T *f, int Ng, T Vinv, T Pshot) {
+    using T2 = vec2_t<T>;
+    const int nh = Ng / 2 + 1;
+    const long n = (long)Ng * Ng * nh;
+    T2 *c = reinterpret_cast<T2 *>(f);
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        if (e == 0) {
+            c[0] = mk2<T2>(0, 0);
+            continue;
+        }
+        const T2 v = c[e];
+        T p;
+        if constexpr (sizeof(T) == 8)
+            p = __dsub_rn(__dmul_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), Vinv), Pshot);
+        else
+            p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+        c[e] = mk2<T2>(p, 0);
+    }
+}
+
+int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStream_t st) {
+    const long n = (long)Ng * Ng * (Ng / 2 + 1);
+    if (prec == 4)
+        power_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, (float)Vinv, (float)Pshot);
+    else
+        power_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, Vinv, Pshot);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+// ---- precision conversion (device grid <-> pinned host view) ---------------------------------
+template <typename D, typename S>
+__global__ void convert_kernel(D *d, const S *__restrict__ s, long n) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        d[e] = (D)s[e];
+}
+
+int convert_grid(void *dst, int dst_prec, const void *src, int src_prec, long n, cudaStream_t st) {
+    if (dst_prec == src_prec) {
+        FG_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * dst_prec, cudaMemcpyDefault, st));
+        return OK;
+    }
+    if (dst_prec == 8)
+        convert_kernel<double, float><<<grid_blocks(n, 256), 256, 0, st>>>((double *)dst, (const float *)src, n);
+    else
+        convert_kernel<float, double><<<grid_blocks(n, 256), 256, 0, st>>>((float *)dst, (const double *)src, n);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+}  // namespace fg

@@ -1,0 +1,101 @@
+/* fftgal_gb300.h -- extensions of the GB300 power-spectrum library beyond the
+ * reference's own C API (include/fft.h, include/power.h, include/gal.h).
+ *
+ * All functions return 0 on success or a negative FFTGAL_ERR_* status; the
+ * message of the last failure on the calling thread is in fftgal_last_error().
+ * Nothing here has a counterpart in the reference unless a citation says so.
+ */
+#ifndef FFTGAL_GB300_H
+#define FFTGAL_GB300_H
+
+#include "fft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFTGAL_OK 0
+#define FFTGAL_ERR_ARG (-1)
+#define FFTGAL_ERR_CUDA (-2)
+#define FFTGAL_ERR_NOMEM (-3)
+#define FFTGAL_ERR_UNSUPPORTED (-4)
+#define FFTGAL_ERR_RANGE (-5)
+#define FFTGAL_ERR_STATE (-6)
+
+/* host-view modes of fft_t.f (see include/fft.h) */
+#define FFTGAL_VIEW_SYNC 0
+#define FFTGAL_VIEW_LAZY 1
+
+/* where caller buffers live */
+#define FFTGAL_MEM_HOST 0
+#define FFTGAL_MEM_DEVICE 1
+
+int fftgal_version(void);
+/* status and message of the last failure on this thread */
+int fftgal_last_status(void);
+const char *fftgal_last_error(void);
+
+/* bytes per grid value on the GPU: 4 (FP32, default) or 8 (FP64).  Chosen at
+ * fft_init from FFTGAL_PRECISION ("f32" | "f64"). */
+int fftgal_grid_precision(const fft_t *grid);
+/* host-view policy; FFTGAL_HOST_VIEW ("sync" | "lazy") sets the default */
+int fftgal_set_host_view(fft_t *grid, int mode);
+/* copy the device grid into grid->f / grid->f into the device grid */
+int fftgal_sync_host(fft_t *grid);
+int fftgal_sync_device(fft_t *grid);
+/* run the grid's work on an existing CUDA stream (cudaStream_t), or NULL to
+ * return to the library's own stream */
+int fftgal_set_stream(fft_t *grid, void *cuda_stream);
+void *fftgal_get_stream(fft_t *grid);
+/* suppress (1) or restore (0) the per-call timing lines on stderr; the
+ * FFTGAL_QUIET environment variable sets the default */
+int fftgal_set_quiet(fft_t *grid, int quiet);
+/* device pointer of the canonical grid (Ng*Ng*Ng_pad values) */
+void *fftgal_device_grid(fft_t *grid);
+/* wait for all queued work of the grid */
+int fftgal_synchronize(fft_t *grid);
+
+/* number of k bins of Pl/Pmu for (Ng, L, dK) (src/power.c:34-36) */
+int fftgal_nk(int Ng, double L, double dK);
+
+/* Interlaced power spectrum of one catalog with FP32 positions in one call:
+ * PCS paint of both interlacing grids in a single particle pass, r2c FFT of
+ * both, offset phase + average + window deconvolution, then multipoles and
+ * Nmu wedges.  Results equal fft_p2k + P + Pl + Pmu (src/fft.c:257-276,
+ * src/power.c:12-178) on the same catalog, with Pmu generalised to Nmu wedges.
+ *   x, y, z   positions [Mpc/h], FP32, on the host or the device (`where`)
+ *   V         catalog volume (shot noise V/Np, normalisation 1/V)
+ *   los       line of sight (normalised internally, not modified)
+ * Outputs (host, any may be NULL): K[NK], N[NK], Pl[NK*4] (l=0,2,4,6);
+ * Kmu[NK*Nmu], Nmu_count[NK*Nmu], Pmu[NK*Nmu].  Bins are normalised exactly as
+ * Pl()/Pmu() normalise them (empty multipole bins are NaN).  The grid is left
+ * holding the deconvolved density field in k space (as after fft_p2k).
+ * Requires an FP32 grid. */
+int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
+                     double V, int where, const double los[3], double dK, int Nmu,
+                     double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
+                     double *Pmu);
+
+/* Per-stage device times (ms) of the last fftgal_power_f32 call, measured with
+ * CUDA events on the grid's stream: [0] position upload, [1] paint key +
+ * histogram, [2] histogram scan, [3] scatter, [4] tile paint, [5] FFT k pass,
+ * [6] FFT j pass, [7] FFT i pass, [8] phase + average + deconvolution,
+ * [9] binning, [10] total.  Enabled with fftgal_set_timing(grid, 1). */
+#define FFTGAL_NSTAGES 11
+int fftgal_set_timing(fft_t *grid, int on);
+int fftgal_stage_times(fft_t *grid, double out_ms[FFTGAL_NSTAGES]);
+/* number of kernel launches the library has issued in this process */
+long fftgal_launch_count(void);
+
+/* PCS readout that sums the 64 stencil terms (the reference's fft_g2p,
+ * src/fft.c:134-169, assigns instead of summing; fft_g2p here reproduces
+ * that).  out[Np] on the host. */
+int fftgal_g2p_sum(fft_t *grid, const gal_t *pos, double *out);
+
+/* bytes of GPU memory held by the grid (grids, scratch, tables) */
+long fftgal_device_bytes(fft_t *grid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

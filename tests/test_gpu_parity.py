@@ -1,0 +1,282 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle and the
+reference's golden outputs.
+
+Tolerances (stated per test):
+  * FP64 grids   : grids and power sums to 1e-12 of the grid's scale; the
+                   octet known answers to the reference's own eps = 1e-15.
+  * FP32 grids   : grids to 2e-5 of their scale; P_l within 1e-4 of
+                   (|P_0^oracle(k)| + Pshot) for k < 0.8 k_Nyq.
+  * mode counts N: bit-exact in every mode; mean K per bin: 1e-12 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from catalogs import uniform_box
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def fg():
+    from fftgal_gb300 import build
+    build.build()
+    import fftgal_gb300
+    return fftgal_gb300
+
+
+@pytest.fixture(scope="module")
+def small():
+    return np.load(os.path.join(GOLD, "small_cases.npz"))
+
+
+def parse_table(text):
+    rows = [[float(t) for t in ln.split()] for ln in str(text).splitlines()
+            if ln and not ln.startswith("#")]
+    return np.array(rows)
+
+
+def grid_close(got, want, rel):
+    scale = max(np.abs(want).max(), 1e-300)
+    err = np.abs(got - want).max() / scale
+    assert err <= rel, f"max error {err:.3e} of scale {scale:.3e} > {rel}"
+
+
+# ---------------------------------------------------------------------------
+# src/tests/octet.c:8-62 through the C ABI
+@pytest.mark.parametrize("prec,eps", [("f64", 1e-15), ("f32", 1e-6)])
+def test_octet_known_answer(fg, prec, eps):
+    g = fg.Grid(2, 2.0, precision=prec)
+    cat = fg.Catalog([-8.0], [-8.0], [-8.0], 8.0)
+    off = g.p2g(cat, [7.0, 7.0, 7.0])
+    assert np.all(off == -1.0) and np.all(g.offset == -1.0)
+    r = g.real
+    for i in range(2):
+        for j in range(2):
+            for k in range(2):
+                assert abs(r[i, j, k] - 8.0 / 27 * (i + 1) * (j + 1) * (k + 1)) < eps
+    g.x2k(1)
+    c = g.cplx
+    for i in range(2):
+        for j in range(2):
+            assert abs(c[i, j, 0].real - 8.0 / (1 + 2 * i) / (1 + 2 * j)) < eps
+            assert abs(c[i, j, 0].imag) < eps
+    g.k2x(0)
+    r = g.real
+    for i in range(2):
+        for j in range(2):
+            for k in range(2):
+                assert abs(r[i, j, k] - 64.0 / 27 / (i + 1) / (j + 1) / (k + 1)) < eps
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("Ng", [2, 3, 4, 5, 6, 7, 8, 12, 16, 30, 32, 64, 96, 128])
+def test_fft_matches_numpy(fg, prec, Ng):
+    rng = np.random.default_rng(Ng)
+    a = rng.standard_normal((Ng, Ng, Ng))
+    g = fg.Grid(Ng, float(Ng), precision=prec)          # L = Ng -> H^3 = 1
+    g.real[..., :Ng] = a
+    g.x2k(0)
+    ref = np.fft.rfftn(a)
+    rel = 1e-13 if prec == "f64" else 2e-6
+    grid_close(g.cplx, ref, rel)
+    g.k2x(0)                                            # c2r / L^3 = identity
+    grid_close(g.real[..., :Ng], a, rel)
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("Ng", [2, 3, 4, 5, 6, 8, 12, 16])
+def test_small_cases_match_reference(fg, oracle_lib, small, prec, Ng):
+    key = f"ng{Ng}"
+    L = float(small[key + "_L"])
+    x, y, z = small[key + "_pos"]
+    xr, yr, zr = small[key + "_rand"]
+    V = L ** 3
+    rel = 1e-12 if prec == "f64" else 2e-5
+    g = fg.Grid(Ng, L, precision=prec)
+    cat = fg.Catalog(x, y, z, V)
+    off = g.p2g(cat, small[key + "_p2g_offset_in"])
+    np.testing.assert_array_equal(off, small[key + "_p2g_offset_out"])
+    grid_close(g.f, small[key + "_p2g"], rel)
+    g.x2k(1)
+    grid_close(g.f, small[key + "_x2k_phase"], rel)
+    g.k2x(1)
+    want = small[key + "_k2x_phase"].reshape(Ng, Ng, -1)[..., :Ng]
+    grid_close(g.real[..., :Ng], want, rel)
+    rcat = fg.Catalog(xr, yr, zr, V)
+    catr = fg.Catalog(x, y, z, V, rand=rcat)
+    g.p2g(catr, [0.0, 0.0, 0.0])
+    grid_close(g.f, small[key + "_p2g_rand"], rel)
+    g.p2k(cat)
+    grid_close(g.f, small[key + "_p2k"], rel)
+    g.power(cat)
+    grid_close(g.f, small[key + "_P"], rel)
+    # Pl/Pmu tables: counts exact, values against the oracle at full precision
+    o = oracle_lib.Oracle(Ng, L)
+    o.p2k(x, y, z, V)
+    o.power(len(x), V)
+    KF = 2 * np.pi / L
+    Pshot = V / len(x)
+    for il, los in enumerate(small["los_set"]):
+        for idk, dK in enumerate((KF, 0.7 * KF, 2.5 * KF)):
+            fpl = f"/tmp/fftgal_test_pl_{os.getpid()}.txt"
+            fmu = f"/tmp/fftgal_test_pmu_{os.getpid()}.txt"
+            losh = g.pl(cat, los, dK, fpl)
+            g.pmu(cat, los, dK, fmu)
+            got = fg.read_table(fpl)
+            gotm = fg.read_table(fmu)
+            ref = parse_table(small[f"{key}_los{il}_dk{idk}_pl"])
+            refm = parse_table(small[f"{key}_los{il}_dk{idk}_pmu"])
+            # counts: bit-exact against the reference's own output
+            np.testing.assert_array_equal(got[:, 1], ref[:, 1])
+            np.testing.assert_array_equal(gotm[:, 1::3], refm[:, 1::3])
+            # the text itself carries 7 significant digits
+            K, N, P, st, losh_o = o.pl(los, dK)
+            np.testing.assert_allclose(losh, losh_o, rtol=0, atol=0)
+            np.testing.assert_allclose(got[:, 0], K, rtol=1e-6, equal_nan=True)
+            den = np.abs(P[:, :1]) + Pshot
+            tol = 1e-6 if prec == "f64" else 1e-4
+            ok = np.isfinite(P)
+            assert np.all(np.isfinite(got[:, 2:]) == ok)
+            assert np.all(np.abs(got[:, 2:] - P)[ok] <= (tol * np.broadcast_to(den, P.shape))[ok] + 1e-300)
+            Km, Nm, Pm, st2, _ = o.pmu(los, dK, 3)
+            np.testing.assert_array_equal(gotm[:, 1::3], Nm)
+            assert np.all(np.abs(gotm[:, 2::3] - Pm) <= tol * (np.abs(Pm) + Pshot))
+
+
+# ---------------------------------------------------------------------------
+def _uniform_ng128():
+    gold = np.load(os.path.join(GOLD, "uniform_ng128.npz"))
+    L, Ng, n = float(gold["L"]), int(gold["Ng"]), int(gold["Np"])
+    x, y, z = uniform_box(int(gold["seed"]), n, L)
+    return gold, L, Ng, n, x, y, z
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_uniform_ng128_capi_matches_reference(fg, prec, tmp_path):
+    """The uniform-box configuration (1e6 particles, Ng=128, interlaced)
+    through the drop-in sequence fft_p2k -> P -> Pl -> Pmu, against the
+    reference's own tables (tests/golden/uniform_ng128.npz)."""
+    gold, L, Ng, n, x, y, z = _uniform_ng128()
+    V = L ** 3
+    Pshot = V / n
+    g = fg.Grid(Ng, L, precision=prec, host_view="lazy")
+    cat = fg.Catalog(x, y, z, V)
+    g.p2k(cat)
+    fk = g.exportf()
+    kny = np.pi * Ng / L
+    for il in range(4):
+        g.importf(fk)
+        g.power(cat)
+        fpl, fmu = str(tmp_path / "pl.txt"), str(tmp_path / "pmu.txt")
+        g.pl(cat, gold[f"los{il}"], 2 * np.pi / L, fpl)
+        g.pmu(cat, gold[f"los{il}"], 2 * np.pi / L, fmu)
+        got, gotm = fg.read_table(fpl), fg.read_table(fmu)
+        ref, refm = parse_table(gold[f"los{il}_pl"]), parse_table(gold[f"los{il}_pmu"])
+        np.testing.assert_array_equal(got[:, 1], ref[:, 1])
+        np.testing.assert_array_equal(gotm[:, 1::3], refm[:, 1::3])
+        np.testing.assert_allclose(got[:, 0], ref[:, 0], rtol=1e-6, equal_nan=True)
+        sel = ref[:, 0] < 0.8 * kny
+        den = np.abs(ref[sel, 2:3]) + Pshot
+        err = np.abs(got[sel, 2:5] - ref[sel, 2:5]) / den
+        assert err.max() <= 1e-4, err.max()
+        errm = np.abs(gotm[sel][:, 2::3] - refm[sel][:, 2::3]) / (np.abs(refm[sel][:, 2::3]) + Pshot)
+        assert errm.max() <= 1e-4, errm.max()
+
+
+def test_uniform_ng128_fused_matches_reference(fg):
+    """The fused single-call path (fftgal_power_f32) on the same catalog."""
+    gold, L, Ng, n, x, y, z = _uniform_ng128()
+    V = L ** 3
+    Pshot = V / n
+    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
+    kny = np.pi * Ng / L
+    for il in range(4):
+        r = g.power_f32(x, y, z, V, gold[f"los{il}"], 2 * np.pi / L, Nmu=3)
+        ref, refm = parse_table(gold[f"los{il}_pl"]), parse_table(gold[f"los{il}_pmu"])
+        np.testing.assert_array_equal(r["N"], ref[:, 1])
+        np.testing.assert_array_equal(r["Nmu"], refm[:, 1::3])
+        sel = ref[:, 0] < 0.8 * kny
+        den = np.abs(ref[sel, 2:3]) + Pshot
+        # FP32 positions: the reference saw FP64 positions of the same points
+        err = np.abs(r["P"][sel, :3] - ref[sel, 2:5]) / den
+        assert err.max() <= 1e-4, err.max()
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("Ng,Nmu", [(16, 3), (30, 10), (64, 10), (33, 4)])
+def test_mode_counts_exact(fg, oracle_lib, small, Ng, Nmu):
+    """N per k bin and per (k, mu) wedge are integers: they must equal the
+    oracle's exactly for every line of sight and bin width."""
+    L = 100.0
+    x, y, z = uniform_box(7, 2000, L)
+    V = L ** 3
+    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
+    o = oracle_lib.Oracle(Ng, L)
+    o.p2k(x, y, z, V)
+    o.power(len(x), V)
+    KF = 2 * np.pi / L
+    for los in small["los_set"]:
+        for dK in (KF, 0.7 * KF, 2.5 * KF):
+            r = g.power_f32(x, y, z, V, los, dK, Nmu=Nmu)
+            K, N, P, st, _ = o.pl(los, dK)
+            Km, Nm, Pm, st2, _ = o.pmu(los, dK, Nmu)
+            np.testing.assert_array_equal(r["N"], N)
+            np.testing.assert_array_equal(r["Nmu"], Nm)
+            np.testing.assert_allclose(r["K"], K, rtol=1e-12, equal_nan=True)
+            np.testing.assert_allclose(r["Kmu"], Km, rtol=1e-12)
+
+
+def test_fp32_paint_is_bit_reproducible(fg):
+    x, y, z = uniform_box(11, 200_000, 500.0)
+    g = fg.Grid(64, 500.0, precision="f32", host_view="lazy")
+    cat = fg.Catalog(x, y, z, 500.0 ** 3)
+    g.p2g(cat, [0.5, 0.5, 0.5])
+    a = g.exportf()
+    g.p2g(cat, [0.5, 0.5, 0.5])
+    b = g.exportf()
+    assert a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_g2p_reference_semantics(fg, oracle_lib, prec):
+    """fft_g2p reproduces the reference (its last stencil term only,
+    src/fft.c:165); fftgal_g2p_sum gives the full PCS interpolation."""
+    Ng, L = 16, 80.0
+    x, y, z = uniform_box(5, 300, L)
+    V = L ** 3
+    g = fg.Grid(Ng, L, precision=prec)
+    cat = fg.Catalog(x, y, z, V)
+    g.p2g(cat, [0.25, -0.5, 0.75])
+    o = oracle_lib.Oracle(Ng, L)
+    o.p2g(x, y, z, V, [0.25, -0.5, 0.75])
+    got = g.g2p(cat)
+    want = o.g2p(x, y, z)
+    rel = 1e-12 if prec == "f64" else 2e-5
+    grid_close(got, want, rel)
+    full = g.g2p_sum(cat)
+    assert np.all(np.isfinite(full)) and np.abs(full).max() > np.abs(got).max()
+
+
+def test_sync_view_sees_host_writes(fg, oracle_lib):
+    """Under the default host view, host writes to F() between calls are seen
+    by the next call (the Psb.c / DLsb.c pattern, src/app/Psb.c:74-84)."""
+    Ng, L = 8, 10.0
+    rng = np.random.default_rng(2)
+    a = rng.standard_normal((Ng, Ng, Ng))
+    g = fg.Grid(Ng, L, precision="f64")
+    g.real[..., :Ng] = a
+    g.x2k(0)
+    g.real[0, 0, 2] *= 3.0        # host edit in k space
+    g.k2x(0)
+    o = oracle_lib.Oracle(Ng, L)
+    o.real[..., :Ng] = a
+    o.x2k(0)
+    o.real[0, 0, 2] *= 3.0
+    o.k2x(0)
+    grid_close(g.real[..., :Ng], o.real[..., :Ng], 1e-12)
