@@ -87,6 +87,7 @@ SIGNATURES = {
     "fftgal_get_stream": (C.c_void_p, [_P_F]),
     "fftgal_set_quiet": (C.c_int, [_P_F, C.c_int]),
     "fftgal_device_grid": (C.c_void_p, [_P_F]),
+    "fftgal_copy_grid": (C.c_int, [_P_F, C.c_void_p, C.c_int]),
     "fftgal_synchronize": (C.c_int, [_P_F]),
     "fftgal_nk": (C.c_int, [C.c_int, C.c_double, C.c_double]),
     "fftgal_power_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
@@ -294,6 +295,14 @@ class Grid:
         out = np.zeros(NSTAGES)
         _check(lib().fftgal_stage_times(self.p, out.ctypes.data_as(_dp)))
         return dict(zip(STAGES, out.tolist()))
+
+    def copy_from(self, ptr: int):
+        """Fill the canonical grid from a CUDA-visible buffer (raw pointer)."""
+        _check(lib().fftgal_copy_grid(self.p, ptr, 1))
+
+    def copy_to(self, ptr: int):
+        """Copy the canonical grid into a CUDA-visible buffer (raw pointer)."""
+        _check(lib().fftgal_copy_grid(self.p, ptr, 0))
 
     def synchronize(self):
         _check(lib().fftgal_synchronize(self.p))

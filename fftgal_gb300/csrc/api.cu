@@ -91,7 +91,7 @@ struct Grid {
     size_t pos_cap = 0;     // bytes
     void *d_stage = nullptr;  // host-double staging for uploads
     size_t stage_cap = 0;
-    double *d_tab = nullptr;  // [3][Ng] complex phase table + [Ng] winv
+    double *d_tab = nullptr;  // [3][Ng] complex phase table, [Ng] winv, [3][Ng] offset-1/2 phase
     BinGeometry geo[kGeoCache];
     int geo_next = 0;
     unsigned long version = 1;  // bumped whenever the grid changes
@@ -215,12 +215,21 @@ static int ensure_aux(Grid *g) {
 
 static int ensure_tables(Grid *g) {
     if (g->d_tab) return OK;
-    FG_CUDA(cudaMalloc(&g->d_tab, sizeof(double) * (7 * (size_t)g->Ng)));
-    std::vector<double> w(g->Ng);
+    const size_t Ng = g->Ng;
+    FG_CUDA(cudaMalloc(&g->d_tab, sizeof(double) * (13 * Ng)));
+    std::vector<double> w(Ng);
     build_winv_table(w.data(), g->Ng);
-    FG_CUDA(cudaMemcpy(g->d_tab + 6 * (size_t)g->Ng, w.data(), sizeof(double) * g->Ng, cudaMemcpyHostToDevice));
+    FG_CUDA(cudaMemcpy(g->d_tab + 6 * Ng, w.data(), sizeof(double) * Ng, cudaMemcpyHostToDevice));
+    // phase table of the interlacing grid (offset 1/2 on every axis, applied)
+    std::vector<double> ph(6 * Ng);
+    const double half[3] = {remainder(0.5, g->Ng), remainder(0.5, g->Ng), remainder(0.5, g->Ng)};
+    build_phase_table(ph.data(), g->Ng, half, 1);
+    FG_CUDA(cudaMemcpy(g->d_tab + 7 * Ng, ph.data(), sizeof(double) * 6 * Ng, cudaMemcpyHostToDevice));
     return OK;
 }
+
+static const double *winv_tab(const Grid *g) { return g->d_tab + 6 * (size_t)g->Ng; }
+static const double *dual_tab(const Grid *g) { return g->d_tab + 7 * (size_t)g->Ng; }
 
 static int phase(Grid *g, void *dst, const double offset[3], int onoff) {
     FG_TRY(ensure_tables(g));
@@ -499,12 +508,9 @@ extern "C" void fft_p2k(fft_t *self, gal_t *part) {
     void *outs[2] = {g->d_f, g->d_aux};
     FG_API(paint_catalog(g, part, outs, offs, 2), "fft_p2k()");
     FG_API(fft_r2c(&g->fft, outs, 2, g->stream), "fft_p2k()");
-    const double H3 = H3_of(g);
-    FG_API(scale_grid(g->d_aux, self->Ng3_pad, g->prec, H3, g->stream), "fft_p2k()");
-    FG_API(phase(g, g->d_aux, offs[1], 1), "fft_p2k()");
-    FG_API(scale_grid(g->d_f, self->Ng3_pad, g->prec, H3, g->stream), "fft_p2k()");
-    FG_API(interlace_average(g->d_f, g->d_aux, self->Ng3_pad, g->prec, g->stream), "fft_p2k()");
-    FG_API(deconv(g, g->d_f), "fft_p2k()");
+    FG_API(ensure_tables(g), "fft_p2k()");
+    FG_API(interlace_finish(g->d_f, g->d_aux, Ng, g->prec, H3_of(g), dual_tab(g), winv_tab(g), g->stream),
+           "fft_p2k()");
     for (int a = 0; a < 3; ++a) self->offset[a] = offs[0][a];
     FG_API(leave(self, true), "fft_p2k()");
     if (!g->quiet) fprintf(stderr, "fft_p2k() %.2fs\n", now_s() - t);
@@ -859,6 +865,20 @@ extern "C" int fftgal_set_quiet(fft_t *grid, int quiet) {
 
 extern "C" void *fftgal_device_grid(fft_t *grid) { return grid ? G(grid)->d_f : nullptr; }
 
+extern "C" int fftgal_copy_grid(fft_t *grid, void *buf, int to_grid) {
+    if (!grid || !buf) return set_error(ERR_ARG, "null argument");
+    Grid *g = G(grid);
+    const size_t bytes = (size_t)g->prec * g->Ng3_pad;
+    if (to_grid) {
+        FG_CUDA(cudaMemcpyAsync(g->d_f, buf, bytes, cudaMemcpyDefault, g->stream));
+        ++g->version;
+    } else {
+        FG_CUDA(cudaMemcpyAsync(buf, g->d_f, bytes, cudaMemcpyDefault, g->stream));
+    }
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    return OK;
+}
+
 extern "C" int fftgal_synchronize(fft_t *grid) {
     if (!grid) return set_error(ERR_ARG, "null grid");
     FG_CUDA(cudaStreamSynchronize(G(grid)->stream));
@@ -938,11 +958,7 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
     FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
-    FG_TRY(scale_grid(g->d_aux, grid->Ng3_pad, 4, H3, st));
-    FG_TRY(phase(g, g->d_aux, spec[1].offset, 1));
-    FG_TRY(scale_grid(g->d_f, grid->Ng3_pad, 4, H3, st));
-    FG_TRY(interlace_average(g->d_f, g->d_aux, grid->Ng3_pad, 4, st));
-    FG_TRY(deconv(g, g->d_f));
+    FG_TRY(interlace_finish(g->d_f, g->d_aux, Ng, 4, H3, dual_tab(g), winv_tab(g), st));
     if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
     for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
     ++g->version;

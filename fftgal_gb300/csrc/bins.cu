@@ -239,6 +239,10 @@ __device__ __forceinline__ bool warp_segsum(int key, float (&v)[NV], int lane) {
     return lane == 31;
 }
 
+// One warp walks one k row (fixed i, j) at a time, 32 modes per step, so the
+// k bin is non-decreasing along the step and the row constants are computed
+// once.  The CTA advances through chunks of kChunkRows rows and folds its FP32
+// partial sums into FP64 after each chunk.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kBinThreads)
 bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
@@ -246,7 +250,7 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
     using T2 = vec2_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int NK = d.NK, W = d.W, NQ = 4 + W;
-    double *acc64 = reinterpret_cast<double *>(smem_raw);          // [NK * NQ]
+    double *acc64 = reinterpret_cast<double *>(smem_raw);               // [NK * NQ]
     float *acc32 = reinterpret_cast<float *>(acc64 + (size_t)NK * NQ);  // [NK * NQ] (FP32 grids)
     uint32_t *thr = reinterpret_cast<uint32_t *>(acc32 + (sizeof(T) == 4 ? (size_t)NK * NQ : 0));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
@@ -257,74 +261,76 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
     for (int e = tid; e < NK + 2; e += blockDim.x) thr[e] = thr_g[e];
     __syncthreads();
 
-    const long nrows = (long)d.Ng * d.Ng;
-    const long nchunks = ceil_div(nrows, kChunkRows);
-    for (long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-        const long e0 = ch * kChunkRows * d.nh;
-        const long e1 = min(nrows, (ch + 1) * kChunkRows) * d.nh;
-        for (long base = e0 + (long)warp * 32; base < e1; base += (long)nwarp * 32) {
-            const long e = base + lane;
-            int b = -1, imu = 0;
-            T pc = 0, mu2t = 0;
-            if (e < e1 && e > 0) {
-                const int k = (int)(e % d.nh);
-                const long row = e / d.nh;
-                const int j = (int)(row % d.Ng), i = (int)(row / d.Ng);
-                const int ki = kval(i, d.Ng), kj = kval(j, d.Ng), kk = kval(k, d.Ng);
-                const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
-                const int count = 1 + ((2 * k) % d.Ng > 0);
-                T p;
-                if constexpr (MODE == 0) {
-                    p = f[row * Ng_pad + 2 * k];
-                } else {
-                    const T2 v = reinterpret_cast<const T2 *>(f)[e];
-                    if constexpr (sizeof(T) == 8)
-                        p = __dsub_rn(__dmul_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), Vinv), Pshot);
-                    else
-                        p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+    const int Ng = d.Ng, nh = d.nh;
+    const int nrows = Ng * Ng;
+    const int nchunks = (nrows + kChunkRows - 1) / kChunkRows;
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int r1 = min(nrows, (ch + 1) * kChunkRows);
+        for (int row = ch * kChunkRows + warp; row < r1; row += nwarp) {
+            const int i = row / Ng, j = row - i * Ng;
+            const int ki = kval(i, Ng), kj = kval(j, Ng);
+            const int n2ij = ki * ki + kj * kj;
+            const T *frow = f + (long)row * Ng_pad;
+            for (int k0 = 0; k0 < nh; k0 += 32) {
+                const int k = k0 + lane;
+                int b = -1, imu = 0;
+                T pc = 0, mu2t = 0;
+                if (k < nh && (row | k) != 0) {
+                    const int kk = kval(k, Ng);
+                    const uint32_t n2 = (uint32_t)(n2ij + kk * kk);
+                    const int count = 1 + ((2 * k) % Ng > 0);
+                    T p;
+                    if constexpr (MODE == 0) {
+                        p = frow[2 * k];
+                    } else {
+                        const T2 v = reinterpret_cast<const T2 *>(frow)[k];
+                        if constexpr (sizeof(T) == 8)
+                            p = __dsub_rn(__dmul_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)), Vinv), Pshot);
+                        else
+                            p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+                    }
+                    pc = p * (T)count;
+                    b = kbin(n2, thr, NK, d.dKinv_f);
+                    if (b >= NK) b = -1;
+                    float mu2f;
+                    imu = wedge_index(ki, kj, kk, sqrtf((float)n2), d, mu2f);
+                    if constexpr (sizeof(T) == 8) {
+                        if (!d.zero_los) {
+                            const double kamp = __dsqrt_rn((double)n2);
+                            const double num = __dadd_rn(__dadd_rn(__dmul_rn((double)ki, d.l0), __dmul_rn((double)kj, d.l1)),
+                                                         __dmul_rn((double)kk, d.l2));
+                            const double mu = __ddiv_rn(num, kamp);
+                            mu2t = __dmul_rn(mu, mu);
+                        }
+                    } else {
+                        mu2t = mu2f;
+                    }
                 }
-                pc = p * (T)count;
-                b = kbin(n2, thr, NK, d.dKinv_f);
-                if (b >= NK) b = -1;
-                const float kampf = sqrtf((float)n2);
-                float mu2f;
-                imu = wedge_index(ki, kj, kk, kampf, d, mu2f);
                 if constexpr (sizeof(T) == 8) {
-                    if (!d.zero_los) {
-                        const double kamp = __dsqrt_rn((double)n2);
-                        const double num = __dadd_rn(__dadd_rn(__dmul_rn((double)ki, d.l0), __dmul_rn((double)kj, d.l1)),
-                                                     __dmul_rn((double)kk, d.l2));
-                        const double mu = __ddiv_rn(num, kamp);
-                        mu2t = __dmul_rn(mu, mu);
+                    if (b >= 0) {
+                        const double m2 = mu2t;
+                        double *a = acc64 + (size_t)b * NQ;
+                        atomicAdd(a + 0, pc);
+                        atomicAdd(a + 1, pc * (1.5 * m2 - 0.5));
+                        atomicAdd(a + 2, pc * ((4.375 * m2 - 3.75) * m2 + 0.375));
+                        atomicAdd(a + 3, pc * (((14.4375 * m2 - 19.6875) * m2 + 6.5625) * m2 - 0.3125));
+                        atomicAdd(a + 4 + imu, pc);
                     }
                 } else {
-                    mu2t = mu2f;
+                    const float m2 = mu2t;
+                    float v[4] = {pc, pc * (1.5f * m2 - 0.5f), pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f),
+                                  pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f)};
+                    if (warp_segsum<4>(b, v, lane) && b >= 0) {
+                        float *a = acc32 + (size_t)b * NQ;
+                        atomicAdd(a + 0, v[0]);
+                        atomicAdd(a + 1, v[1]);
+                        atomicAdd(a + 2, v[2]);
+                        atomicAdd(a + 3, v[3]);
+                    }
+                    float w[1] = {pc};
+                    const int wkey = b < 0 ? -1 : b * W + imu;
+                    if (warp_segsum<1>(wkey, w, lane) && wkey >= 0) atomicAdd(acc32 + (size_t)b * NQ + 4 + imu, w[0]);
                 }
-            }
-            if constexpr (sizeof(T) == 8) {
-                if (b >= 0) {
-                    const double m2 = mu2t;
-                    double *a = acc64 + (size_t)b * NQ;
-                    atomicAdd(a + 0, pc);
-                    atomicAdd(a + 1, pc * (1.5 * m2 - 0.5));
-                    atomicAdd(a + 2, pc * ((4.375 * m2 - 3.75) * m2 + 0.375));
-                    atomicAdd(a + 3, pc * (((14.4375 * m2 - 19.6875) * m2 + 6.5625) * m2 - 0.3125));
-                    atomicAdd(a + 4 + imu, pc);
-                }
-            } else {
-                const float m2 = mu2t;
-                float v[4] = {pc, pc * (1.5f * m2 - 0.5f), pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f),
-                              pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f)};
-                if (warp_segsum<4>(b, v, lane) && b >= 0) {
-                    float *a = acc32 + (size_t)b * NQ;
-                    atomicAdd(a + 0, v[0]);
-                    atomicAdd(a + 1, v[1]);
-                    atomicAdd(a + 2, v[2]);
-                    atomicAdd(a + 3, v[3]);
-                }
-                float w[1] = {pc};
-                const int wkey = b < 0 ? -1 : b * W + imu;
-                if (warp_segsum<1>(wkey, w, lane) && wkey >= 0) atomicAdd(acc32 + (size_t)b * NQ + 4 + imu, w[0]);
             }
         }
         if constexpr (sizeof(T) == 4) {

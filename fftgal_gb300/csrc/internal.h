@@ -80,6 +80,11 @@ int fft_c2r(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_k_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
 int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
+// two-level FP32 kernels (fft2.cu) for power-of-two Ng in [4, 1024]
+bool fft2_supported(int Ng, int prec);
+int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
+              long nbatch, int sign, cudaStream_t s);
+int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s);
 // i-axis pass of two grids fused with the interlacing finish:
 // A <- scale * 0.5 * (A + B * phaseB) * Winv3   (see spectral tables)
 int fft_pass_i_interlace(const FftPlan *p, void *gridA, void *gridB,
@@ -134,6 +139,10 @@ int apply_phase(void *f, int Ng, int prec, const void *d_tab, cudaStream_t st);
 int build_winv_table(double *host_tab, int Ng);
 int apply_deconv(void *f, int Ng, int prec, const void *d_winv, cudaStream_t st);
 int interlace_average(void *f, const void *fdual, long n, int prec, cudaStream_t st);
+// A <- deconv(0.5 * (phase(B * H3) + A * H3)) in one pass; d_tab is the
+// [3][Ng] phase table of B's offset, d_winv the [Ng] deconvolution table
+int interlace_finish(void *A, const void *B, int Ng, int prec, double H3, const void *d_tab,
+                     const void *d_winv, cudaStream_t st);
 int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStream_t st);
 int convert_grid(void *dst, int dst_prec, const void *src, int src_prec, long n, cudaStream_t st);
 

@@ -18,10 +18,13 @@
 //               accumulates their weights in shared memory and writes every
 //               owned cell exactly once (no global atomics, no zeroing pass).
 //
-// FP32 grids accumulate in 64-bit fixed point (2^-32 of a particle's weight):
-// integer sums are order independent, so the painted grid is bit-reproducible
-// run to run.  FP64 grids reproduce the reference's FP64 weight arithmetic op
-// for op and accumulate in FP64.
+// FP32 grids accumulate in 32-bit fixed point with a per-tile scale 2^-s,
+// s chosen from the tile's particle count so that no cell sum can overflow
+// (a particle adds at most (2/3)^3 of its weight to one cell).  Integer sums
+// are order independent, so the painted grid is bit-reproducible run to run;
+// 32-bit shared-memory integer atomics are native, unlike 64-bit ones.  FP64
+// grids reproduce the reference's FP64 weight arithmetic op for op and
+// accumulate in FP64.
 #include "internal.h"
 #include "common.cuh"
 
@@ -33,7 +36,8 @@ namespace fg {
 
 constexpr int kTileMax = 16;
 constexpr int kMaxPaintGrids = 2;
-constexpr double kFix = 4294967296.0;  // 2^32
+constexpr double kMaxCellWeight = 8.0 / 27.0;  // largest PCS weight product
+constexpr int kMinFixBits = 8;                   // below this: FP32 accumulation
 
 struct AxisParams {
     // FP32 path: x * h - o as double-float (h = Ng/L, o = offset of grid g)
@@ -277,7 +281,7 @@ struct PaintOut {
 };
 
 template <typename G> struct Acc;
-template <> struct Acc<float> { using type = unsigned long long; };
+template <> struct Acc<float> { using type = unsigned int; };
 template <> struct Acc<double> { using type = double; };
 
 template <typename G>
@@ -291,6 +295,7 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
     __shared__ int nseg_s;
+    __shared__ int fixbits_s;
 
     const int Ng = pp.Ng, nt = pp.nt;
     const int tx = blockIdx.x / (nt * nt), ty = (blockIdx.x / nt) % nt, tz = blockIdx.x % nt;
@@ -342,10 +347,17 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
                 }
         seg_pref[ns] = pref;
         nseg_s = ns;
+        // fixed-point bits: total * kMaxCellWeight * 2^s < 2^32
+        int fb = 31;
+        if (pref > 0) fb = (int)floor(log2(4294967295.0 / ((double)pref * kMaxCellWeight)));
+        fixbits_s = fb > 31 ? 31 : fb;
     }
     __syncthreads();
     const int nseg = nseg_s;
     const uint32_t total = seg_pref[nseg];
+    const int fixbits = fixbits_s;
+    const bool fixed = fixbits >= kMinFixBits;  // false only for > 5e7 particles
+    const float fscale = ldexpf(1.0f, fixbits);
 
     for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
         int lo = 0, hi = nseg - 1;
@@ -385,8 +397,10 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
                         if (loc[2][k] < 0) continue;
                         if constexpr (sizeof(G) == 4) {
                             const float wv = wij * w[2][k];
-                            atomicAdd(&acc[g * T3 + rowb + loc[2][k]],
-                                      (unsigned long long)__float2ll_rn(wv * 4294967296.0f));
+                            if (fixed)
+                                atomicAdd(&acc[g * T3 + rowb + loc[2][k]], __float2uint_rn(wv * fscale));
+                            else
+                                atomicAdd(reinterpret_cast<float *>(&acc[g * T3 + rowb + loc[2][k]]), wv);
                         } else {
                             atomicAdd(&acc[g * T3 + rowb + loc[2][k]], __dmul_rn(wij, w[2][k]));
                         }
@@ -404,7 +418,7 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
     const int ncell = te[0] * te[1] * rowlen;
     for (int g = 0; g < ngr; ++g) {
         G *out = reinterpret_cast<G *>(po.out[g]);
-        const G sc = sizeof(G) == 4 ? (G)(po.scale[g] / kFix) : (G)po.scale[g];
+        const G sc = sizeof(G) == 4 ? (G)ldexp(po.scale[g], fixed ? -fixbits : 0) : (G)po.scale[g];
         const int accu = po.accumulate[g];
         for (int e = threadIdx.x; e < ncell; e += blockDim.x) {
             const int lk = e % rowlen, lj = (e / rowlen) % te[1], li = e / (rowlen * te[1]);
@@ -413,7 +427,7 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
             if (lk < te[2]) {
                 const A a = acc[g * T3 + (li * kTileMax + lj) * kTileMax + lk];
                 if constexpr (sizeof(G) == 4)
-                    v = __ull2float_rn(a) * sc;
+                    v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
                 else
                     v = a * sc;
             }
@@ -562,7 +576,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt * t->nt * t->nt);
-    const size_t smem = (size_t)ngrids * kTileMax * kTileMax * kTileMax * 8;
+    const size_t smem = (size_t)ngrids * kTileMax * kTileMax * kTileMax * (grid_prec == 4 ? 4 : 8);
     if (grid_prec == 4) {
         FG_CUDA(cudaFuncSetAttribute(paint_tile_kernel<float>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -22,6 +22,26 @@ static unsigned grid_blocks(long n, int threads) {
     return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
+// Half-spectrum modes are visited in chunks of kRowChunk rows (row = i*Ng+j)
+// so every index is 32-bit: e = chunk offset + q, q < kRowChunk*nh.
+constexpr int kRowChunk = 16;
+
+static unsigned chunk_blocks(int Ng) {
+    const long nchunks = ceil_div((long)Ng * Ng, kRowChunk);
+    const long cap = 32L * num_sms();
+    return (unsigned)(nchunks < cap ? nchunks : cap);
+}
+
+#define FG_FOR_MODES(Ng, nh)                                                                \
+    for (int ch_ = blockIdx.x; ch_ * kRowChunk < (Ng) * (Ng); ch_ += gridDim.x)             \
+        for (int q_ = threadIdx.x, row0_ = ch_ * kRowChunk,                                 \
+                 qn_ = min(kRowChunk, (Ng) * (Ng) - ch_ * kRowChunk) * (nh);                \
+             q_ < qn_; q_ += blockDim.x)                                                   \
+            if (const int rl_ = q_ / (nh); true)                                            \
+                if (const int k = q_ - rl_ * (nh), row = row0_ + rl_; true)                 \
+                    if (const int i = row / (Ng), j = row - i * (Ng); true)                 \
+                        if (const long e = (long)row * (nh) + k; true)
+
 // ---- scale -------------------------------------------------------------------
 template <typename T>
 __global__ void scale_kernel(T *f, long n, T s) {
@@ -88,10 +108,8 @@ __global__ void phase_kernel(T *f, int Ng, const double *__restrict__ tab) {
     const int nh = Ng / 2 + 1;
     const long n = (long)Ng * Ng * nh;
     T2 *c = reinterpret_cast<T2 *>(f);
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        const int k = (int)(e % nh);
-        const long row = e / nh;
-        const int j = (int)(row % Ng), i = (int)(row / Ng);
+    (void)n;
+    FG_FOR_MODES(Ng, nh) {
         T pr, pi;
         phase_of<T>(tab, Ng, i, j, k, pr, pi);
         const T2 v = c[e];
@@ -106,9 +124,10 @@ __global__ void phase_kernel(T *f, int Ng, const double *__restrict__ tab) {
 int apply_phase(void *f, int Ng, int prec, const void *d_tab, cudaStream_t st) {
     const long n = (long)Ng * Ng * (Ng / 2 + 1);
     if (prec == 4)
-        phase_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, (const double *)d_tab);
+        phase_kernel<float><<<chunk_blocks(Ng), 256, 0, st>>>((float *)f, Ng, (const double *)d_tab);
     else
-        phase_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, (const double *)d_tab);
+        phase_kernel<double><<<chunk_blocks(Ng), 256, 0, st>>>((double *)f, Ng, (const double *)d_tab);
+    (void)n;
     FG_LAUNCHED(1);
     return OK;
 }
@@ -132,10 +151,8 @@ __global__ void deconv_kernel(T *f, int Ng, const double *__restrict__ winv) {
     const int nh = Ng / 2 + 1;
     const long n = (long)Ng * Ng * nh;
     T2 *c = reinterpret_cast<T2 *>(f);
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
-        const int k = (int)(e % nh);
-        const long row = e / nh;
-        const int j = (int)(row % Ng), i = (int)(row / Ng);
+    (void)n;
+    FG_FOR_MODES(Ng, nh) {
         const T2 v = c[e];
         if constexpr (sizeof(T) == 8) {
             const double w3 = __dmul_rn(__dmul_rn(winv[i], winv[j]), winv[k]);
@@ -150,9 +167,10 @@ __global__ void deconv_kernel(T *f, int Ng, const double *__restrict__ winv) {
 int apply_deconv(void *f, int Ng, int prec, const void *d_winv, cudaStream_t st) {
     const long n = (long)Ng * Ng * (Ng / 2 + 1);
     if (prec == 4)
-        deconv_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, (const double *)d_winv);
+        deconv_kernel<float><<<chunk_blocks(Ng), 256, 0, st>>>((float *)f, Ng, (const double *)d_winv);
     else
-        deconv_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, (const double *)d_winv);
+        deconv_kernel<double><<<chunk_blocks(Ng), 256, 0, st>>>((double *)f, Ng, (const double *)d_winv);
+    (void)n;
     FG_LAUNCHED(1);
     return OK;
 }
@@ -177,6 +195,50 @@ int interlace_average(void *f, const void *fdual, long n, int prec, cudaStream_t
     return OK;
 }
 
+// ---- fused interlacing finish ---------------------------------------------------------
+// A <- deconv(0.5 * (phase(B * H3) + A * H3)): the tail of src/fft.c:257-276
+// (x2k scale of both grids, offset phase of the dual grid, average, PCS
+// deconvolution) in one pass that reads both grids and writes one.  FP64
+// evaluates each step in the reference's order.
+template <typename T>
+__global__ void finish_kernel(T *A, const T *__restrict__ B, int Ng, T H3, const double *__restrict__ tab,
+                              const double *__restrict__ winv) {
+    using T2 = vec2_t<T>;
+    const int nh = Ng / 2 + 1;
+    T2 *a = reinterpret_cast<T2 *>(A);
+    const T2 *b = reinterpret_cast<const T2 *>(B);
+    FG_FOR_MODES(Ng, nh) {
+        T pr, pi;
+        phase_of<T>(tab, Ng, i, j, k, pr, pi);
+        const T2 bv = b[e], av = a[e];
+        if constexpr (sizeof(T) == 8) {
+            const double br = __dmul_rn(bv.x, H3), bi = __dmul_rn(bv.y, H3);
+            const double dr = __dsub_rn(__dmul_rn(br, pr), __dmul_rn(bi, pi));
+            const double di = __dadd_rn(__dmul_rn(br, pi), __dmul_rn(bi, pr));
+            const double mr = __dmul_rn(0.5, __dadd_rn(dr, __dmul_rn(av.x, H3)));
+            const double mi = __dmul_rn(0.5, __dadd_rn(di, __dmul_rn(av.y, H3)));
+            const double w3 = __dmul_rn(__dmul_rn(winv[i], winv[j]), winv[k]);
+            a[e] = mk2<T2>(__dmul_rn(mr, w3), __dmul_rn(mi, w3));
+        } else {
+            const float dr = bv.x * pr - bv.y * pi, di = bv.x * pi + bv.y * pr;
+            const float w3 = (float)(winv[i] * winv[j] * winv[k]) * (0.5f * H3);
+            a[e] = mk2<T2>((dr + av.x) * w3, (di + av.y) * w3);
+        }
+    }
+}
+
+int interlace_finish(void *A, const void *B, int Ng, int prec, double H3, const void *d_tab,
+                     const void *d_winv, cudaStream_t st) {
+    if (prec == 4)
+        finish_kernel<float><<<chunk_blocks(Ng), 256, 0, st>>>((float *)A, (const float *)B, Ng, (float)H3,
+                                                             (const double *)d_tab, (const double *)d_winv);
+    else
+        finish_kernel<double><<<chunk_blocks(Ng), 256, 0, st>>>((double *)A, (const double *)B, Ng, H3,
+                                                              (const double *)d_tab, (const double *)d_winv);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
 // ---- P(): |delta|^2 / V - Pshot in place ---------------------------------------------------
 template <typename T>
 __global__ void power_kernel(T *f, int Ng, T Vinv, T Pshot) {
@@ -184,7 +246,10 @@ __global__ void power_kernel(T *f, int Ng, T Vinv, T Pshot) {
     const int nh = Ng / 2 + 1;
     const long n = (long)Ng * Ng * nh;
     T2 *c = reinterpret_cast<T2 *>(f);
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    (void)n;
+    FG_FOR_MODES(Ng, nh) {
+        (void)i;
+        (void)j;
         if (e == 0) {
             c[0] = mk2<T2>(0, 0);
             continue;
@@ -202,9 +267,10 @@ __global__ void power_kernel(T *f, int Ng, T Vinv, T Pshot) {
 int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStream_t st) {
     const long n = (long)Ng * Ng * (Ng / 2 + 1);
     if (prec == 4)
-        power_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, (float)Vinv, (float)Pshot);
+        power_kernel<float><<<chunk_blocks(Ng), 256, 0, st>>>((float *)f, Ng, (float)Vinv, (float)Pshot);
     else
-        power_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, Vinv, Pshot);
+        power_kernel<double><<<chunk_blocks(Ng), 256, 0, st>>>((double *)f, Ng, Vinv, Pshot);
+    (void)n;
     FG_LAUNCHED(1);
     return OK;
 }

@@ -52,6 +52,10 @@ void *fftgal_get_stream(fft_t *grid);
 int fftgal_set_quiet(fft_t *grid, int quiet);
 /* device pointer of the canonical grid (Ng*Ng*Ng_pad values) */
 void *fftgal_device_grid(fft_t *grid);
+/* copy Ng3_pad values of the grid's precision between the canonical grid and
+ * a caller buffer (host or device, any CUDA-visible pointer):
+ * to_grid = 1 copies buf -> grid, 0 copies grid -> buf */
+int fftgal_copy_grid(fft_t *grid, void *buf, int to_grid);
 /* wait for all queued work of the grid */
 int fftgal_synchronize(fft_t *grid);
 

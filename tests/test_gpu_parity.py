@@ -280,3 +280,28 @@ def test_sync_view_sees_host_writes(fg, oracle_lib):
     o.real[0, 0, 2] *= 3.0
     o.k2x(0)
     grid_close(g.real[..., :Ng], o.real[..., :Ng], 1e-12)
+
+
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("Ng", [256, 512, 1024])
+def test_fft_large_matches_cufft(fg, Ng):
+    """Large FP32 transforms against cuFFT in FP64 (torch.fft, a cross-check
+    only): relative error to the largest mode <= 2e-6."""
+    torch = pytest.importorskip("torch")
+    Ngp = 2 * (Ng // 2 + 1)
+    g = fg.Grid(Ng, float(Ng), precision="f32", host_view="lazy")   # H^3 = 1
+    gen = torch.Generator(device="cuda").manual_seed(Ng)
+    x = torch.randn((Ng, Ng, Ngp), generator=gen, device="cuda", dtype=torch.float32)
+    g.copy_from(x.data_ptr())
+    g.x2k(0)
+    out = torch.empty_like(x)
+    g.copy_to(out.data_ptr())
+    got = torch.view_as_complex(out.view(Ng, Ng, Ngp // 2, 2))
+    ref = torch.fft.rfftn(x[..., :Ng].double())
+    err = ((got.to(torch.complex128) - ref).abs().max() / ref.abs().max()).item()
+    del ref
+    assert err <= 2e-6, err
+    g.k2x(0)                         # back: c2r / L^3 = identity
+    g.copy_to(out.data_ptr())
+    back_err = ((out[..., :Ng] - x[..., :Ng]).abs().max() / x.abs().max()).item()
+    assert back_err <= 2e-6, back_err
