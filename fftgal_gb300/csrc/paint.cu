@@ -296,6 +296,7 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
     __shared__ int nseg_s;
     __shared__ int fixbits_s;
+    __shared__ int wrapped_s;
 
     const int Ng = pp.Ng, nt = pp.nt;
     const int tx = blockIdx.x / (nt * nt), ty = (blockIdx.x / nt) % nt, tz = blockIdx.x % nt;
@@ -347,69 +348,92 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
                 }
         seg_pref[ns] = pref;
         nseg_s = ns;
-        // fixed-point bits: total * kMaxCellWeight * 2^s < 2^32
+        // first try: fixed-point bits for a generous bound on one cell's
+        // particle count (four times the mean count of a 4^3 stencil window
+        // plus 64); a wrapped cell sum is detected and the tile redone with
+        // the bound `pref` (every particle in one cell), which cannot wrap
+        const double mean_win = 64.0 * pref / ((double)te[0] * te[1] * te[2]);
+        const double cnt = fmin((double)pref, 4.0 * mean_win + 64.0);
         int fb = 31;
-        if (pref > 0) fb = (int)floor(log2(4294967295.0 / ((double)pref * kMaxCellWeight)));
+        if (pref > 0) fb = (int)floor(log2(4294967295.0 / (cnt * kMaxCellWeight)));
         fixbits_s = fb > 31 ? 31 : fb;
+        wrapped_s = 0;
     }
     __syncthreads();
     const int nseg = nseg_s;
     const uint32_t total = seg_pref[nseg];
-    const int fixbits = fixbits_s;
-    const bool fixed = fixbits >= kMinFixBits;  // false only for > 5e7 particles
-    const float fscale = ldexpf(1.0f, fixbits);
+    int fixbits = fixbits_s;
+    bool fixed = fixbits >= kMinFixBits;  // false only for > 5e7 particles in a tile
 
-    for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
-        int lo = 0, hi = nseg - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (seg_pref[mid] <= q) lo = mid; else hi = mid - 1;
-        }
-        const auto r = sorted[seg_begin[lo] + (q - seg_pref[lo])];
-        const G pos[3] = {(G)r.x, (G)r.y, (G)r.z};
-        for (int g = 0; g < ngr; ++g) {
-            int loc[3][4];
-            G w[3][4];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                int b;
-                G d;
-                coord(pos[a], pp.ax[a], g, Ng, b, d);
-                pcs_weights(d, w[a]);
-#pragma unroll
-                for (int s = 0; s < 4; ++s) {
-                    int c = b - 1 + s;
-                    c = c < 0 ? c + Ng : (c >= Ng ? c - Ng : c);
-                    const int l = c - t0[a];
-                    loc[a][s] = (l >= 0 && l < te[a]) ? l : -1;
-                }
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const float fscale = ldexpf(1.0f, fixbits);
+        bool wrapped = false;
+        for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
+            int lo = 0, hi = nseg - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (seg_pref[mid] <= q) lo = mid; else hi = mid - 1;
             }
+            const auto r = sorted[seg_begin[lo] + (q - seg_pref[lo])];
+            const G pos[3] = {(G)r.x, (G)r.y, (G)r.z};
+            for (int g = 0; g < ngr; ++g) {
+                int loc[3][4];
+                G w[3][4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                if (loc[0][i] < 0) continue;
+                for (int a = 0; a < 3; ++a) {
+                    int b;
+                    G d;
+                    coord(pos[a], pp.ax[a], g, Ng, b, d);
+                    pcs_weights(d, w[a]);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (loc[1][j] < 0) continue;
-                    const G wij = w[0][i] * w[1][j];
-                    const int rowb = (loc[0][i] * kTileMax + loc[1][j]) * kTileMax;
+                    for (int s = 0; s < 4; ++s) {
+                        int c = b - 1 + s;
+                        c = c < 0 ? c + Ng : (c >= Ng ? c - Ng : c);
+                        const int l = c - t0[a];
+                        loc[a][s] = (l >= 0 && l < te[a]) ? l : -1;
+                    }
+                }
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        if (loc[2][k] < 0) continue;
-                        if constexpr (sizeof(G) == 4) {
-                            const float wv = wij * w[2][k];
-                            if (fixed)
-                                atomicAdd(&acc[g * T3 + rowb + loc[2][k]], __float2uint_rn(wv * fscale));
-                            else
-                                atomicAdd(reinterpret_cast<float *>(&acc[g * T3 + rowb + loc[2][k]]), wv);
-                        } else {
-                            atomicAdd(&acc[g * T3 + rowb + loc[2][k]], __dmul_rn(wij, w[2][k]));
+                for (int i = 0; i < 4; ++i) {
+                    if (loc[0][i] < 0) continue;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (loc[1][j] < 0) continue;
+                        const G wij = w[0][i] * w[1][j];
+                        const int rowb = (loc[0][i] * kTileMax + loc[1][j]) * kTileMax;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            if (loc[2][k] < 0) continue;
+                            if constexpr (sizeof(G) == 4) {
+                                const float wv = wij * w[2][k];
+                                if (fixed) {
+                                    const unsigned v = __float2uint_rn(wv * fscale);
+                                    const unsigned old = atomicAdd(&acc[g * T3 + rowb + loc[2][k]], v);
+                                    wrapped |= (old + v < old);
+                                } else {
+                                    atomicAdd(reinterpret_cast<float *>(&acc[g * T3 + rowb + loc[2][k]]), wv);
+                                }
+                            } else {
+                                atomicAdd(&acc[g * T3 + rowb + loc[2][k]], __dmul_rn(wij, w[2][k]));
+                            }
                         }
                     }
                 }
             }
         }
+        if (wrapped) wrapped_s = 1;
+        __syncthreads();
+        const bool redo = wrapped_s && attempt == 0;
+        __syncthreads();
+        if (!redo) break;
+        if (threadIdx.x == 0) wrapped_s = 0;
+        // a cell sum wrapped: redo with the bound that cannot wrap
+        fixbits = (int)floor(log2(4294967295.0 / ((double)total * kMaxCellWeight)));
+        fixbits = fixbits > 31 ? 31 : fixbits;
+        fixed = fixbits >= kMinFixBits;
+        for (int e = threadIdx.x; e < ngr * T3; e += blockDim.x) acc[e] = (A)0;
+        __syncthreads();
     }
-    __syncthreads();
 
     // write the owned cells (and the row padding of the last k tile)
     const bool last_k = (t0[2] + te[2] == Ng);
