@@ -869,13 +869,15 @@ extern "C" int fftgal_copy_grid(fft_t *grid, void *buf, int to_grid) {
     if (!grid || !buf) return set_error(ERR_ARG, "null argument");
     Grid *g = G(grid);
     const size_t bytes = (size_t)g->prec * g->Ng3_pad;
+    // finish the grid's own work, then copy synchronously on the legacy
+    // default stream so the copy also follows the caller's default-stream work
+    FG_CUDA(cudaStreamSynchronize(g->stream));
     if (to_grid) {
-        FG_CUDA(cudaMemcpyAsync(g->d_f, buf, bytes, cudaMemcpyDefault, g->stream));
+        FG_CUDA(cudaMemcpy(g->d_f, buf, bytes, cudaMemcpyDefault));
         ++g->version;
     } else {
-        FG_CUDA(cudaMemcpyAsync(buf, g->d_f, bytes, cudaMemcpyDefault, g->stream));
+        FG_CUDA(cudaMemcpy(buf, g->d_f, bytes, cudaMemcpyDefault));
     }
-    FG_CUDA(cudaStreamSynchronize(g->stream));
     return OK;
 }
 

@@ -54,7 +54,9 @@ int fftgal_set_quiet(fft_t *grid, int quiet);
 void *fftgal_device_grid(fft_t *grid);
 /* copy Ng3_pad values of the grid's precision between the canonical grid and
  * a caller buffer (host or device, any CUDA-visible pointer):
- * to_grid = 1 copies buf -> grid, 0 copies grid -> buf */
+ * to_grid = 1 copies buf -> grid, 0 copies grid -> buf.  The copy waits for
+ * the grid's stream and runs on the legacy default stream; work that fills
+ * `buf` on other non-blocking streams must be complete first. */
 int fftgal_copy_grid(fft_t *grid, void *buf, int to_grid);
 /* wait for all queued work of the grid */
 int fftgal_synchronize(fft_t *grid);

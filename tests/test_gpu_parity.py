@@ -286,7 +286,8 @@ def test_sync_view_sees_host_writes(fg, oracle_lib):
 @pytest.mark.parametrize("Ng", [256, 512, 1024])
 def test_fft_large_matches_cufft(fg, Ng):
     """Large FP32 transforms against cuFFT in FP64 (torch.fft, a cross-check
-    only): relative error to the largest mode <= 2e-6."""
+    only): relative L2 error <= 1e-6 and largest error <= 1e-5 of the largest
+    mode (FP32 rounding grows like log2 N)."""
     torch = pytest.importorskip("torch")
     Ngp = 2 * (Ng // 2 + 1)
     g = fg.Grid(Ng, float(Ng), precision="f32", host_view="lazy")   # H^3 = 1
@@ -298,10 +299,14 @@ def test_fft_large_matches_cufft(fg, Ng):
     g.copy_to(out.data_ptr())
     got = torch.view_as_complex(out.view(Ng, Ng, Ngp // 2, 2))
     ref = torch.fft.rfftn(x[..., :Ng].double())
-    err = ((got.to(torch.complex128) - ref).abs().max() / ref.abs().max()).item()
-    del ref
-    assert err <= 2e-6, err
+    diff = got.to(torch.complex128) - ref
+    err_max = (diff.abs().max() / ref.abs().max()).item()
+    err_l2 = (torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(ref)).item()
+    del ref, diff
+    assert err_l2 <= 1e-6 and err_max <= 1e-5, (err_l2, err_max)
     g.k2x(0)                         # back: c2r / L^3 = identity
     g.copy_to(out.data_ptr())
-    back_err = ((out[..., :Ng] - x[..., :Ng]).abs().max() / x.abs().max()).item()
-    assert back_err <= 2e-6, back_err
+    d = (out[..., :Ng] - x[..., :Ng]).double()
+    back_l2 = (torch.linalg.vector_norm(d) / torch.linalg.vector_norm(x[..., :Ng].double())).item()
+    back_max = (d.abs().max() / x.abs().max()).item()
+    assert back_l2 <= 1e-6 and back_max <= 1e-5, (back_l2, back_max)
