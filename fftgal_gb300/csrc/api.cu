@@ -382,7 +382,7 @@ extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
     FG_API(cuda_check(cudaMalloc(&g->d_f, (size_t)g->prec * self->Ng3_pad), "grid"), "fft_init()");
     FG_API(cuda_check(cudaMemsetAsync(g->d_f, 0, (size_t)g->prec * self->Ng3_pad, g->stream), "grid"), "fft_init()");
     FG_API(fft_plan_create(&g->fft, Ng, g->prec), "fft_init()");
-    FG_API(paint_tiling_create(&g->tiling, Ng, 16), "fft_init()");
+    FG_API(paint_tiling_create(&g->tiling, Ng), "fft_init()");
     FG_API(cuda_check(cudaStreamSynchronize(g->stream), "init"), "fft_init()");
     const bool estimate = wisdom && !strcmp(wisdom, "FFTW_ESTIMATE");
     if (estimate) {
@@ -395,8 +395,8 @@ extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
         } else {
             fp = fopen(wisdom, "w");
             if (fp) {
-                fprintf(fp, "fftgal_gb300 plan Ng=%d prec=%d cols=%d rows=%d tile=%d\n", Ng, g->prec,
-                        g->fft.cols, g->fft.rows, g->tiling.tmax);
+                fprintf(fp, "fftgal_gb300 plan Ng=%d prec=%d cols=%d rows=%d tile=%dx%dx%d\n", Ng, g->prec,
+                        g->fft.cols, g->fft.rows, g->tiling.tmax[0], g->tiling.tmax[1], g->tiling.tmax[2]);
                 fclose(fp);
                 fprintf(stderr, "fft_init() exported plan to %s\n", wisdom);
             }

@@ -347,6 +347,106 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
         if (acc64[e] != 0) atomicAdd(&gacc[e], acc64[e]);
 }
 
+// FP32 grids: one thread per contiguous run of kSegModes modes of a k row.
+// Along k the k bin is non-decreasing, so the thread keeps running sums in
+// registers and flushes them to shared memory only when the bin (or, for the
+// wedge sums, the (bin, wedge) pair) changes.  Shared accumulators are laid
+// out [quantity][bin] so neighbouring bins fall in neighbouring banks.
+constexpr int kSegModes = 16;
+
+template <int MODE>
+__global__ void __launch_bounds__(kBinThreads)
+bin_power_seg_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Pshot,
+                     const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, int Ng_pad) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int NK = d.NK, W = d.W, NQ = 4 + W;
+    double *acc64 = reinterpret_cast<double *>(smem_raw);               // [NQ][NK]
+    float *acc32 = reinterpret_cast<float *>(acc64 + (size_t)NK * NQ);  // [NQ][NK]
+    uint32_t *thr = reinterpret_cast<uint32_t *>(acc32 + (size_t)NK * NQ);
+    const int tid = threadIdx.x;
+    for (int e = tid; e < NK * NQ; e += blockDim.x) {
+        acc64[e] = 0;
+        acc32[e] = 0.f;
+    }
+    for (int e = tid; e < NK + 2; e += blockDim.x) thr[e] = thr_g[e];
+    __syncthreads();
+
+    const int Ng = d.Ng, nh = d.nh;
+    const int nrows = Ng * Ng;
+    const int nsegr = (nh + kSegModes - 1) / kSegModes;
+    const int nchunks = (nrows + kChunkRows - 1) / kChunkRows;
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int r0 = ch * kChunkRows;
+        const int nitems = (min(nrows, r0 + kChunkRows) - r0) * nsegr;
+        for (int it = tid; it < nitems; it += blockDim.x) {
+            const int row = r0 + it / nsegr, seg = it % nsegr;
+            const int i = row / Ng, j = row - i * Ng;
+            const int ki = kval(i, Ng), kj = kval(j, Ng);
+            const int n2ij = ki * ki + kj * kj;
+            const float *frow = f + (long)row * Ng_pad;
+            int cb = -1, cw = -1;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, sw = 0.f;
+            const int k1 = min(nh, (seg + 1) * kSegModes);
+            for (int k = seg * kSegModes; k < k1; ++k) {
+                if ((row | k) == 0) continue;  // the k = 0 mode (src/power.c:52-54)
+                const int kk = kval(k, Ng);
+                const uint32_t n2 = (uint32_t)(n2ij + kk * kk);
+                float p;
+                if constexpr (MODE == 0) {
+                    p = frow[2 * k];
+                } else {
+                    const float2 v = reinterpret_cast<const float2 *>(frow)[k];
+                    p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+                }
+                const float pc = (2 * k) % Ng > 0 ? 2.f * p : p;
+                int b = kbin(n2, thr, NK, d.dKinv_f);
+                if (b >= NK) b = -1;
+                float m2;
+                const int imu = wedge_index(ki, kj, kk, sqrtf((float)n2), d, m2);
+                if (b != cb) {
+                    if (cb >= 0) {
+                        atomicAdd(acc32 + 0 * NK + cb, s0);
+                        atomicAdd(acc32 + 1 * NK + cb, s1);
+                        atomicAdd(acc32 + 2 * NK + cb, s2);
+                        atomicAdd(acc32 + 3 * NK + cb, s3);
+                    }
+                    cb = b;
+                    s0 = s1 = s2 = s3 = 0.f;
+                }
+                s0 += pc;
+                s1 += pc * (1.5f * m2 - 0.5f);
+                s2 += pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f);
+                s3 += pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f);
+                const int wk = b < 0 ? -1 : b * W + imu;
+                if (wk != cw) {
+                    if (cw >= 0) atomicAdd(acc32 + (4 + cw % W) * NK + cw / W, sw);
+                    cw = wk;
+                    sw = 0.f;
+                }
+                sw += pc;
+            }
+            if (cb >= 0) {
+                atomicAdd(acc32 + 0 * NK + cb, s0);
+                atomicAdd(acc32 + 1 * NK + cb, s1);
+                atomicAdd(acc32 + 2 * NK + cb, s2);
+                atomicAdd(acc32 + 3 * NK + cb, s3);
+            }
+            if (cw >= 0) atomicAdd(acc32 + (4 + cw % W) * NK + cw / W, sw);
+        }
+        __syncthreads();
+        for (int e = tid; e < NK * NQ; e += blockDim.x) {
+            acc64[e] += (double)acc32[e];
+            acc32[e] = 0.f;
+        }
+        __syncthreads();
+    }
+    // back to the [bin][quantity] layout of the global accumulators
+    for (int e = tid; e < NK * NQ; e += blockDim.x) {
+        const int q = e / NK, b = e - q * NK;
+        if (acc64[e] != 0) atomicAdd(&gacc[(size_t)b * NQ + q], acc64[e]);
+    }
+}
+
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
               double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end) {
     if (!g->valid) return set_error(ERR_STATE, "bin geometry not built");
@@ -359,7 +459,8 @@ int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, do
     FG_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(double) * g->acc_len, st));
     const int Ng_pad = 2 * (s.Ng / 2 + 1);
     const long nchunks = ceil_div((long)s.Ng * s.Ng, kChunkRows);
-    int per_sm = smem > 110 * 1024 ? 1 : 2;
+    int per_sm = (int)((220 * 1024) / smem);
+    per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
     long nb = (long)num_sms() * per_sm;
     if (nb > nchunks) nb = nchunks;
 #define FG_BIN_LAUNCH(T, M)                                                                            \
@@ -370,7 +471,15 @@ int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, do
             d, (const T *)f, (T)Vinv, (T)Pshot, g->d_thr, g->d_acc, Ng_pad);                           \
     } while (0)
     if (prec == 4) {
-        if (mode == 0) FG_BIN_LAUNCH(float, 0); else FG_BIN_LAUNCH(float, 1);
+        if (mode == 0) {
+            FG_CUDA(cudaFuncSetAttribute(bin_power_seg_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            bin_power_seg_kernel<0><<<(unsigned)nb, kBinThreads, smem, st>>>(d, (const float *)f, (float)Vinv,
+                                                                            (float)Pshot, g->d_thr, g->d_acc, Ng_pad);
+        } else {
+            FG_CUDA(cudaFuncSetAttribute(bin_power_seg_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            bin_power_seg_kernel<1><<<(unsigned)nb, kBinThreads, smem, st>>>(d, (const float *)f, (float)Vinv,
+                                                                            (float)Pshot, g->d_thr, g->d_acc, Ng_pad);
+        }
     } else {
         if (mode == 0) FG_BIN_LAUNCH(double, 0); else FG_BIN_LAUNCH(double, 1);
     }

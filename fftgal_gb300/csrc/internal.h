@@ -94,10 +94,11 @@ int fft_pass_i_interlace(const FftPlan *p, void *gridA, void *gridB,
 // ---- paint -----------------------------------------------------------------
 struct PaintTiling {
     int Ng = 0;
-    int nt = 0;                   // tiles per axis
-    int tmax = 0;                 // largest tile extent
-    int *d_tables = nullptr;      // device: tile_of[Ng], start[nt+1]
-    long nkeys = 0;               // nt^3 * 27
+    int nt[3] = {0, 0, 0};        // tiles along i, j, k
+    int tmax[3] = {0, 0, 0};      // largest tile extent along i, j, k
+    int *d_tables = nullptr;      // device, per axis a: tile_of[Ng], then start[nt[a]+1]
+    int tab_off[3] = {0, 0, 0};   // offset of axis a's tables in d_tables
+    long nkeys = 0;               // nt0*nt1*nt2 * 27
 };
 
 struct PaintScratch {
@@ -118,7 +119,7 @@ struct PaintGridSpec {
     int accumulate = 0;           // 0: overwrite (and zero padding), 1: out += value
 };
 
-int paint_tiling_create(PaintTiling *t, int Ng, int tile);
+int paint_tiling_create(PaintTiling *t, int Ng);
 void paint_tiling_destroy(PaintTiling *t);
 void paint_scratch_free(PaintScratch *s);
 

@@ -6,11 +6,11 @@
 // organisation is new:
 //
 //  1. key     : every particle gets the key (tile, class) of its base cell.  The
-//               grid is cut into <= 16^3-cell tiles; per axis the class says
-//               whether the particle's stencil (over all painted grids) reaches
-//               into the lower (1) or upper (2) neighbour tile, or neither (0).
-//               The rank of the particle within its key comes from the
-//               histogram atomic.
+//               grid is cut into tiles of at most 16 x 16 x 32 cells (i, j, k);
+//               per axis the class says whether the particle's stencil (over
+//               all painted grids) reaches into the lower (1) or upper (2)
+//               neighbour tile, or neither (0).  The rank of the particle
+//               within its key comes from the histogram atomic.
 //  2. scan    : exclusive prefix sum of the key histogram.
 //  3. scatter : particles are written in key order.
 //  4. paint   : one CTA per tile owns its cells.  It pulls the particles of its
@@ -18,13 +18,17 @@
 //               accumulates their weights in shared memory and writes every
 //               owned cell exactly once (no global atomics, no zeroing pass).
 //
-// FP32 grids accumulate in 32-bit fixed point with a per-tile scale 2^-s,
-// s chosen from the tile's particle count so that no cell sum can overflow
-// (a particle adds at most (2/3)^3 of its weight to one cell).  Integer sums
-// are order independent, so the painted grid is bit-reproducible run to run;
-// 32-bit shared-memory integer atomics are native, unlike 64-bit ones.  FP64
-// grids reproduce the reference's FP64 weight arithmetic op for op and
-// accumulate in FP64.
+// FP32 grids (paint_coop_kernel): each lane prepares one particle (cell
+// indices and the 3 x 4 weights of both grids) in shared memory, then the warp
+// deposits the particles one at a time with lane = (grid, i row, j row), each
+// lane adding its 4 k cells.  The shared layout puts those 32 rows in 32
+// distinct banks.  Sums are 32-bit fixed point with a per-tile scale 2^-s: a
+// first pass counts particles per 4^3-cell block, and s is the largest value
+// for which no cell can exceed 2^32 (a particle adds at most (2/3)^3 of its
+// weight to a cell).  Integer sums are order independent, so the painted grid
+// is bit-reproducible run to run.
+// FP64 grids (paint_tile_f64_kernel) reproduce the reference's FP64 weight
+// arithmetic op for op and accumulate in FP64, one thread per particle.
 #include "internal.h"
 #include "common.cuh"
 
@@ -34,10 +38,21 @@
 
 namespace fg {
 
-constexpr int kTileMax = 16;
+constexpr int kTileExt[3] = {16, 16, 32};    // i, j, k
 constexpr int kMaxPaintGrids = 2;
 constexpr double kMaxCellWeight = 8.0 / 27.0;  // largest PCS weight product
-constexpr int kMinFixBits = 8;                   // below this: FP32 accumulation
+constexpr int kMinFixBits = 8;                 // below this: FP32 accumulation
+// FP32 shared layout: cell (li, lj, lk) of grid g at g*kGS + li*kSI + lj*kSJ + lk;
+// kSJ = 1, kSI = 4, kGS = 16 (mod 32) gives the 32 rows (g, li+a, lj+b),
+// a, b < 4, of one stencil 32 distinct banks.
+constexpr int kSJ = 33, kSI = 548, kGS = 8784;
+static_assert(15 * kSI + 15 * kSJ + 31 < kGS, "tile does not fit the layout");
+// FP64 shared layout: dense [16][16][32]
+constexpr int kT3 = 16 * 16 * 32;
+// per-tile block counts: 4^3-cell blocks over the tile plus a 4-cell margin
+constexpr int kBlk = 4;
+__host__ __device__ constexpr int blk_dim(int a) { return a == 2 ? (32 + 8) / kBlk : (16 + 8) / kBlk; }  // 6, 6, 10
+constexpr int kBlkN = blk_dim(0) * blk_dim(1) * blk_dim(2);
 
 struct AxisParams {
     // FP32 path: x * h - o as double-float (h = Ng/L, o = offset of grid g)
@@ -50,15 +65,15 @@ struct AxisParams {
 
 struct PaintParams {
     AxisParams ax[3];
-    int Ng, Ng_pad, nt, ngrids;
-    const int *tile_of;   // [Ng]
-    const int *start;     // [nt + 1]
+    int Ng, Ng_pad, ngrids;
+    int nt[3];
+    const int *tile_of[3];   // [Ng] per axis
+    const int *start[3];     // [nt + 1] per axis
 };
 
 // ---- per-axis cell coordinate ----------------------------------------------
 
-__device__ __forceinline__ void coord(float x, const AxisParams &a, int g, int Ng, int &b,
-                                      float &d) {
+__device__ __forceinline__ void coord(float x, const AxisParams &a, int g, int Ng, int &b, float &d) {
     // u = x*h - o with the rounding errors of the product and the subtraction
     // carried in a second float, then split into floor and fraction
     const float p = x * a.h_hi;
@@ -83,8 +98,7 @@ __device__ __forceinline__ void coord(float x, const AxisParams &a, int g, int N
     d = fr;
 }
 
-__device__ __forceinline__ void coord(double x, const AxisParams &a, int g, int Ng, int &b,
-                                      double &d) {
+__device__ __forceinline__ void coord(double x, const AxisParams &a, int g, int Ng, int &b, double &d) {
     // src/fft.c:68-82, evaluated without contraction so it rounds like the host
     const double u = __dsub_rn(__dmul_rn(x, a.h), a.o[g]);
     const int g1 = (int)floor(u);
@@ -113,6 +127,15 @@ __device__ __forceinline__ void pcs_weights(double d, double w[4]) {
     w[3] = __ddiv_rn(__dmul_rn(d2, d), 6.0);
 }
 
+// local index of stencil cell s (0..3) of base cell b: (b - 1 + s) mod Ng
+// relative to the tile start t0, or -1 outside [0, te)
+__device__ __forceinline__ int local_cell(int b, int s, int Ng, int t0, int te) {
+    int c = b - 1 + s;
+    c = c < 0 ? c + Ng : (c >= Ng ? c - Ng : c);
+    const int l = c - t0;
+    return (l >= 0 && l < te) ? l : -1;
+}
+
 template <typename P> struct Rec;
 template <> struct Rec<float> { using type = float4; };
 template <> struct Rec<double> { struct type { double x, y, z; }; };
@@ -124,7 +147,7 @@ __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ 
                                  const P *__restrict__ z, long Np, PaintParams pp,
                                  uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                                  uint32_t *__restrict__ hist) {
-    const int Ng = pp.Ng, nt = pp.nt;
+    const int Ng = pp.Ng;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np;
          p += (long)gridDim.x * blockDim.x) {
         const P pos[3] = {x[p], y[p], z[p]};
@@ -134,9 +157,9 @@ __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ 
             int b0;
             P d;
             coord(pos[a], pp.ax[a], 0, Ng, b0, d);
-            const int ta = pp.tile_of[b0];
-            const int t0 = pp.start[ta];
-            const int te = pp.start[ta + 1] - t0;
+            const int ta = pp.tile_of[a][b0];
+            const int t0 = pp.start[a][ta];
+            const int te = pp.start[a][ta + 1] - t0;
             int rmin = b0 - t0, rmax = b0 - t0;
             for (int g = 1; g < pp.ngrids; ++g) {
                 int bg;
@@ -147,10 +170,10 @@ __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ 
                 rmax = max(rmax, b0 - t0 + dl);
             }
             t[a] = ta;
-            cls[a] = nt == 1 ? 0 : (rmin - 1 < 0 ? 1 : (rmax + 2 >= te ? 2 : 0));
+            cls[a] = pp.nt[a] == 1 ? 0 : (rmin - 1 < 0 ? 1 : (rmax + 2 >= te ? 2 : 0));
         }
-        const uint32_t k =
-            (uint32_t)((((long)t[0] * nt + t[1]) * nt + t[2]) * 27 + cls[0] * 9 + cls[1] * 3 + cls[2]);
+        const uint32_t k = (uint32_t)((((long)t[0] * pp.nt[1] + t[1]) * pp.nt[2] + t[2]) * 27 + cls[0] * 9 +
+                                      cls[1] * 3 + cls[2]);
         key[p] = k;
         rank[p] = atomicAdd(&hist[k], 1u);
     }
@@ -162,8 +185,7 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
 constexpr int kScanBlock = kScanThreads * kScanPer;
 
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *warp_sums,
-                                                         uint32_t *total) {
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *warp_sums, uint32_t *total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t inc = v;
 #pragma unroll
@@ -280,183 +302,306 @@ struct PaintOut {
     int accumulate[kMaxPaintGrids];
 };
 
-template <typename G> struct Acc;
-template <> struct Acc<float> { using type = unsigned int; };
-template <> struct Acc<double> { using type = double; };
-
-template <typename G>
-__global__ void __launch_bounds__(kPaintThreads)
-paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
-                  const typename Rec<G>::type *__restrict__ sorted, PaintOut po) {
-    using A = typename Acc<G>::type;
-    constexpr int T3 = kTileMax * kTileMax * kTileMax;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    A *acc = reinterpret_cast<A *>(smem_raw);  // [ngrids][T3]
-    __shared__ uint32_t seg_begin[kMaxSeg];
-    __shared__ uint32_t seg_pref[kMaxSeg + 1];
-    __shared__ int nseg_s;
-    __shared__ int fixbits_s;
-    __shared__ int wrapped_s;
-
-    const int Ng = pp.Ng, nt = pp.nt;
-    const int tx = blockIdx.x / (nt * nt), ty = (blockIdx.x / nt) % nt, tz = blockIdx.x % nt;
-    const int tt[3] = {tx, ty, tz};
+// Tile geometry and the flattened list of particle segments a tile pulls:
+// its own key range for every class and the boundary classes of the (up to
+// 26, deduplicated for 1 or 2 tiles per axis) neighbours.
+struct TileSegs {
     int t0[3], te[3];
+    int nseg;
+    uint32_t total;
+};
+
+__device__ void tile_segments(const PaintParams &pp, const uint32_t *__restrict__ off, uint32_t *seg_begin,
+                              uint32_t *seg_pref, uint32_t *scan_ws, TileSegs &ts) {
+    const int nt0 = pp.nt[0], nt1 = pp.nt[1], nt2 = pp.nt[2];
+    const int tt[3] = {(int)(blockIdx.x / (nt1 * nt2)), (int)((blockIdx.x / nt2) % nt1), (int)(blockIdx.x % nt2)};
+    (void)nt0;
+    int nopt[3], otile[3][5], ocls[3][5];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        t0[a] = pp.start[tt[a]];
-        te[a] = pp.start[tt[a] + 1] - t0[a];
-    }
-    const int ngr = pp.ngrids;
-    for (int e = threadIdx.x; e < ngr * T3; e += blockDim.x) acc[e] = (A)0;
-
-    if (threadIdx.x == 0) {
-        // per axis: list of (neighbour tile, class mask)
-        int nopt[3], otile[3][5], ocls[3][5];
-        for (int a = 0; a < 3; ++a) {
-            int k = 0;
-            if (nt == 1) {
-                otile[a][k] = tt[a]; ocls[a][k++] = 0;
-            } else {
-                // own tile: all classes
-                for (int c = 0; c < 3; ++c) { otile[a][k] = tt[a]; ocls[a][k++] = c; }
-                const int lo = (tt[a] + nt - 1) % nt, hi = (tt[a] + 1) % nt;
-                if (nt == 2) {
-                    otile[a][k] = hi; ocls[a][k++] = 1;
-                    otile[a][k] = hi; ocls[a][k++] = 2;
-                } else {
-                    otile[a][k] = lo; ocls[a][k++] = 2;  // lower tile, reaching up
-                    otile[a][k] = hi; ocls[a][k++] = 1;  // upper tile, reaching down
-                }
+        ts.t0[a] = pp.start[a][tt[a]];
+        ts.te[a] = pp.start[a][tt[a] + 1] - ts.t0[a];
+        const int nt = pp.nt[a];
+        int k = 0;
+        if (nt == 1) {
+            otile[a][k] = tt[a];
+            ocls[a][k++] = 0;
+        } else {
+            for (int c = 0; c < 3; ++c) {
+                otile[a][k] = tt[a];
+                ocls[a][k++] = c;
             }
-            nopt[a] = k;
+            const int lo = (tt[a] + nt - 1) % nt, hi = (tt[a] + 1) % nt;
+            if (nt == 2) {
+                otile[a][k] = hi;
+                ocls[a][k++] = 1;
+                otile[a][k] = hi;
+                ocls[a][k++] = 2;
+            } else {
+                otile[a][k] = lo;  // lower tile, particles reaching up
+                ocls[a][k++] = 2;
+                otile[a][k] = hi;  // upper tile, particles reaching down
+                ocls[a][k++] = 1;
+            }
         }
-        int ns = 0;
-        uint32_t pref = 0;
-        for (int i = 0; i < nopt[0]; ++i)
-            for (int j = 0; j < nopt[1]; ++j)
-                for (int k = 0; k < nopt[2]; ++k) {
-                    const long key = (((long)otile[0][i] * nt + otile[1][j]) * nt + otile[2][k]) * 27 +
-                                     ocls[0][i] * 9 + ocls[1][j] * 3 + ocls[2][k];
-                    const uint32_t b = off[key], e = off[key + 1];
-                    if (e > b) {
-                        seg_begin[ns] = b;
-                        seg_pref[ns] = pref;
-                        pref += e - b;
-                        ++ns;
-                    }
-                }
-        seg_pref[ns] = pref;
-        nseg_s = ns;
-        // first try: fixed-point bits for a generous bound on one cell's
-        // particle count (four times the mean count of a 4^3 stencil window
-        // plus 64); a wrapped cell sum is detected and the tile redone with
-        // the bound `pref` (every particle in one cell), which cannot wrap
-        const double mean_win = 64.0 * pref / ((double)te[0] * te[1] * te[2]);
-        const double cnt = fmin((double)pref, 4.0 * mean_win + 64.0);
-        int fb = 31;
-        if (pref > 0) fb = (int)floor(log2(4294967295.0 / (cnt * kMaxCellWeight)));
-        fixbits_s = fb > 31 ? 31 : fb;
-        wrapped_s = 0;
+        nopt[a] = k;
+    }
+    const int ncomb = nopt[0] * nopt[1] * nopt[2];  // <= 125
+    const int q = threadIdx.x;
+    uint32_t b = 0, cnt = 0;
+    if (q < ncomb) {
+        const int i = q / (nopt[1] * nopt[2]), j = (q / nopt[2]) % nopt[1], k = q % nopt[2];
+        const long key = (((long)otile[0][i] * nt1 + otile[1][j]) * nt2 + otile[2][k]) * 27 + ocls[0][i] * 9 +
+                         ocls[1][j] * 3 + ocls[2][k];
+        b = off[key];
+        cnt = off[key + 1] - b;
+    }
+    uint32_t tot;
+    const uint32_t pref = block_exclusive_scan(cnt, scan_ws, &scan_ws[31]);
+    tot = scan_ws[31];
+    if (q < ncomb) {
+        seg_begin[q] = b;
+        seg_pref[q] = pref;
+    }
+    if (q == 0) seg_pref[ncomb] = tot;
+    __syncthreads();
+    ts.nseg = ncomb;
+    ts.total = seg_pref[ncomb];
+}
+
+// index of particle q of the flattened segment list (largest segment whose
+// prefix is <= q; empty segments are skipped automatically)
+__device__ __forceinline__ uint32_t seg_index(uint32_t q, const uint32_t *seg_begin, const uint32_t *seg_pref,
+                                              int nseg) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (seg_pref[mid] <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return seg_begin[lo] + (q - seg_pref[lo]);
+}
+
+struct StageRec {
+    uint32_t loc[3];  // per axis: 4 packed local cell indices (255 = outside the tile)
+    float w[3][4];    // per axis: PCS weights
+};
+
+__device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int l = local_cell(b, s, Ng, t0, te);
+        r |= (uint32_t)(l < 0 ? 255 : l) << (8 * s);
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(kPaintThreads, 2)
+paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4 *__restrict__ sorted,
+                  PaintOut po) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS]
+    StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS);  // [warps][32][grids]
+    uint32_t *blk = reinterpret_cast<uint32_t *>(stage + (kPaintThreads / 32) * 32 * kMaxPaintGrids);  // [kBlkN]
+    __shared__ uint32_t seg_begin[kMaxSeg];
+    __shared__ uint32_t seg_pref[kMaxSeg + 1];
+    __shared__ uint32_t scan_ws[32];
+    __shared__ int fixbits_s;
+
+    const int Ng = pp.Ng, ngr = pp.ngrids;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    for (int e = tid; e < ngr * kGS; e += blockDim.x) acc[e] = 0u;
+    for (int e = tid; e < kBlkN; e += blockDim.x) blk[e] = 0u;
+    TileSegs ts;
+    tile_segments(pp, off, seg_begin, seg_pref, scan_ws, ts);
+    const uint32_t total = ts.total;
+    const int nseg = ts.nseg;
+
+    // pass A: particles per 4^3 block of base cells (tile plus a 4-cell margin)
+    for (uint32_t q = tid; q < total; q += blockDim.x) {
+        const float4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+        const float pos[3] = {r.x, r.y, r.z};
+        int bidx = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int b;
+            float d;
+            coord(pos[a], pp.ax[a], 0, Ng, b, d);
+            int l = b - ts.t0[a];
+            if (l > Ng / 2) l -= Ng;
+            if (l < -Ng / 2) l += Ng;
+            int bb = (l + 4) / kBlk;  // margin of 4 cells below the tile
+            bb = bb < 0 ? 0 : (bb >= blk_dim(a) ? blk_dim(a) - 1 : bb);
+            bidx = bidx * blk_dim(a) + bb;
+        }
+        atomicAdd(&blk[bidx], 1u);
     }
     __syncthreads();
-    const int nseg = nseg_s;
-    const uint32_t total = seg_pref[nseg];
-    int fixbits = fixbits_s;
-    bool fixed = fixbits >= kMinFixBits;  // false only for > 5e7 particles in a tile
+    // a cell's contributors have grid-0 base cells within 3 below to 2 above
+    // it per axis: at most 3 consecutive blocks per axis
+    if (tid < 32) {
+        uint32_t mx = 0;
+        for (int e = lane; e < kBlkN; e += 32) {
+            const int bk = e % blk_dim(2), bj = (e / blk_dim(2)) % blk_dim(1), bi = e / (blk_dim(2) * blk_dim(1));
+            if (bi + 2 >= blk_dim(0) || bj + 2 >= blk_dim(1) || bk + 2 >= blk_dim(2)) continue;
+            uint32_t s = 0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    for (int c = 0; c < 3; ++c) s += blk[((bi + a) * blk_dim(1) + bj + b) * blk_dim(2) + bk + c];
+            mx = max(mx, s);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) {
+            // a tile of one axis-wrapping extent can see a particle twice per
+            // axis through the periodic images: bound by the total instead
+            const bool wraps = ts.te[0] == Ng || ts.te[1] == Ng || ts.te[2] == Ng;
+            const double cnt = wraps ? (double)total : (double)mx;
+            int fb = 31;
+            if (cnt > 0) fb = (int)floor(log2(4294967295.0 / (cnt * kMaxCellWeight)));
+            fixbits_s = fb > 31 ? 31 : fb;
+        }
+    }
+    __syncthreads();
+    const int fixbits = fixbits_s;
+    const bool fixed = fixbits >= kMinFixBits;
+    const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
 
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        const float fscale = ldexpf(1.0f, fixbits);
-        bool wrapped = false;
-        for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
-            int lo = 0, hi = nseg - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (seg_pref[mid] <= q) lo = mid; else hi = mid - 1;
-            }
-            const auto r = sorted[seg_begin[lo] + (q - seg_pref[lo])];
-            const G pos[3] = {(G)r.x, (G)r.y, (G)r.z};
+    // pass B: stage 32 particles per warp, then deposit them one by one
+    const int g_l = lane >> 4, a_l = (lane >> 2) & 3, b_l = lane & 3;
+    StageRec *mystage = stage + warp * 32 * kMaxPaintGrids;
+    for (uint32_t base = (uint32_t)warp * 32; base < total; base += (uint32_t)nwarp * 32) {
+        const uint32_t q = base + lane;
+        if (q < total) {
+            const float4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+            const float pos[3] = {r.x, r.y, r.z};
             for (int g = 0; g < ngr; ++g) {
-                int loc[3][4];
-                G w[3][4];
+                StageRec &st = mystage[lane * kMaxPaintGrids + g];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
                     int b;
-                    G d;
+                    float d;
                     coord(pos[a], pp.ax[a], g, Ng, b, d);
-                    pcs_weights(d, w[a]);
+                    float w[4];
+                    pcs_weights(d, w);
+                    st.loc[a] = pack_local(b, Ng, ts.t0[a], ts.te[a]);
 #pragma unroll
-                    for (int s = 0; s < 4; ++s) {
-                        int c = b - 1 + s;
-                        c = c < 0 ? c + Ng : (c >= Ng ? c - Ng : c);
-                        const int l = c - t0[a];
-                        loc[a][s] = (l >= 0 && l < te[a]) ? l : -1;
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    if (loc[0][i] < 0) continue;
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        if (loc[1][j] < 0) continue;
-                        const G wij = w[0][i] * w[1][j];
-                        const int rowb = (loc[0][i] * kTileMax + loc[1][j]) * kTileMax;
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            if (loc[2][k] < 0) continue;
-                            if constexpr (sizeof(G) == 4) {
-                                const float wv = wij * w[2][k];
-                                if (fixed) {
-                                    const unsigned v = __float2uint_rn(wv * fscale);
-                                    const unsigned old = atomicAdd(&acc[g * T3 + rowb + loc[2][k]], v);
-                                    wrapped |= (old + v < old);
-                                } else {
-                                    atomicAdd(reinterpret_cast<float *>(&acc[g * T3 + rowb + loc[2][k]]), wv);
-                                }
-                            } else {
-                                atomicAdd(&acc[g * T3 + rowb + loc[2][k]], __dmul_rn(wij, w[2][k]));
-                            }
-                        }
-                    }
+                    for (int s = 0; s < 4; ++s) st.w[a][s] = w[s] * (a == 2 ? fscale : 1.f);
                 }
             }
         }
-        if (wrapped) wrapped_s = 1;
-        __syncthreads();
-        const bool redo = wrapped_s && attempt == 0;
-        __syncthreads();
-        if (!redo) break;
-        if (threadIdx.x == 0) wrapped_s = 0;
-        // a cell sum wrapped: redo with the bound that cannot wrap
-        fixbits = (int)floor(log2(4294967295.0 / ((double)total * kMaxCellWeight)));
-        fixbits = fixbits > 31 ? 31 : fixbits;
-        fixed = fixbits >= kMinFixBits;
-        for (int e = threadIdx.x; e < ngr * T3; e += blockDim.x) acc[e] = (A)0;
-        __syncthreads();
+        __syncwarp();
+        const int np = min(32u, total - base);
+        if (g_l < ngr) {
+            for (int p = 0; p < np; ++p) {
+                const StageRec &st = mystage[p * kMaxPaintGrids + g_l];
+                const int li = (st.loc[0] >> (8 * a_l)) & 255, lj = (st.loc[1] >> (8 * b_l)) & 255;
+                if (li == 255 || lj == 255) continue;
+                const float wij = st.w[0][a_l] * st.w[1][b_l];
+                uint32_t *row = acc + g_l * kGS + li * kSI + lj * kSJ;
+                const uint32_t lk = st.loc[2];
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const uint32_t l = (lk >> (8 * s)) & 255;
+                    if (l == 255) continue;
+                    const float wv = wij * st.w[2][s];
+                    if (fixed)
+                        atomicAdd(row + l, __float2uint_rn(wv));
+                    else
+                        atomicAdd(reinterpret_cast<float *>(row + l), wv);
+                }
+            }
+        }
+        __syncwarp();
     }
+    __syncthreads();
 
     // write the owned cells (and the row padding of the last k tile)
-    const bool last_k = (t0[2] + te[2] == Ng);
+    const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
     const int pad = last_k ? pp.Ng_pad - Ng : 0;
-    const int rowlen = te[2] + pad;
-    const int ncell = te[0] * te[1] * rowlen;
+    const int rowlen = ts.te[2] + pad;
+    const int ncell = ts.te[0] * ts.te[1] * rowlen;
     for (int g = 0; g < ngr; ++g) {
-        G *out = reinterpret_cast<G *>(po.out[g]);
-        const G sc = sizeof(G) == 4 ? (G)ldexp(po.scale[g], fixed ? -fixbits : 0) : (G)po.scale[g];
+        float *out = reinterpret_cast<float *>(po.out[g]);
+        const float sc = (float)ldexp(po.scale[g], fixed ? -fixbits : 0);
         const int accu = po.accumulate[g];
-        for (int e = threadIdx.x; e < ncell; e += blockDim.x) {
-            const int lk = e % rowlen, lj = (e / rowlen) % te[1], li = e / (rowlen * te[1]);
-            const long gi = ((long)(t0[0] + li) * Ng + (t0[1] + lj)) * pp.Ng_pad + t0[2] + lk;
-            G v = 0;
-            if (lk < te[2]) {
-                const A a = acc[g * T3 + (li * kTileMax + lj) * kTileMax + lk];
-                if constexpr (sizeof(G) == 4)
-                    v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
-                else
-                    v = a * sc;
+        for (int e = tid; e < ncell; e += blockDim.x) {
+            const int lk = e % rowlen, lj = (e / rowlen) % ts.te[1], li = e / (rowlen * ts.te[1]);
+            const long gi = ((long)(ts.t0[0] + li) * Ng + (ts.t0[1] + lj)) * pp.Ng_pad + ts.t0[2] + lk;
+            float v = 0.f;
+            if (lk < ts.te[2]) {
+                const uint32_t a = acc[g * kGS + li * kSI + lj * kSJ + lk];
+                v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
             }
             if (accu) {
-                if (lk < te[2]) out[gi] += v;
+                if (lk < ts.te[2]) out[gi] += v;
+            } else {
+                out[gi] = v;
+            }
+        }
+    }
+}
+
+// FP64 grids: one thread per particle, FP64 shared atomics
+__global__ void __launch_bounds__(kPaintThreads)
+paint_tile_f64_kernel(PaintParams pp, const uint32_t *__restrict__ off,
+                      const Rec<double>::type *__restrict__ sorted, PaintOut po) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *acc = reinterpret_cast<double *>(smem_raw);  // [ngrids][kT3], dense [16][16][32]
+    __shared__ uint32_t seg_begin[kMaxSeg];
+    __shared__ uint32_t seg_pref[kMaxSeg + 1];
+    __shared__ uint32_t scan_ws[32];
+    const int Ng = pp.Ng, ngr = pp.ngrids;
+    for (int e = threadIdx.x; e < ngr * kT3; e += blockDim.x) acc[e] = 0.0;
+    TileSegs ts;
+    tile_segments(pp, off, seg_begin, seg_pref, scan_ws, ts);
+    for (uint32_t q = threadIdx.x; q < ts.total; q += blockDim.x) {
+        const auto r = sorted[seg_index(q, seg_begin, seg_pref, ts.nseg)];
+        const double pos[3] = {r.x, r.y, r.z};
+        for (int g = 0; g < ngr; ++g) {
+            int loc[3][4];
+            double w[3][4];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                int b;
+                double d;
+                coord(pos[a], pp.ax[a], g, Ng, b, d);
+                pcs_weights(d, w[a]);
+#pragma unroll
+                for (int s = 0; s < 4; ++s) loc[a][s] = local_cell(b, s, Ng, ts.t0[a], ts.te[a]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (loc[0][i] < 0) continue;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (loc[1][j] < 0) continue;
+                    const double wij = __dmul_rn(w[0][i], w[1][j]);
+                    double *row = acc + g * kT3 + (loc[0][i] * 16 + loc[1][j]) * 32;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (loc[2][k] >= 0) atomicAdd(row + loc[2][k], __dmul_rn(wij, w[2][k]));
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
+    const int pad = last_k ? pp.Ng_pad - Ng : 0;
+    const int rowlen = ts.te[2] + pad;
+    const int ncell = ts.te[0] * ts.te[1] * rowlen;
+    for (int g = 0; g < ngr; ++g) {
+        double *out = reinterpret_cast<double *>(po.out[g]);
+        const double sc = po.scale[g];
+        const int accu = po.accumulate[g];
+        for (int e = threadIdx.x; e < ncell; e += blockDim.x) {
+            const int lk = e % rowlen, lj = (e / rowlen) % ts.te[1], li = e / (rowlen * ts.te[1]);
+            const long gi = ((long)(ts.t0[0] + li) * Ng + (ts.t0[1] + lj)) * pp.Ng_pad + ts.t0[2] + lk;
+            double v = 0;
+            if (lk < ts.te[2]) v = __dmul_rn(acc[g * kT3 + (li * 16 + lj) * 32 + lk], sc);
+            if (accu) {
+                if (lk < ts.te[2]) out[gi] = __dadd_rn(out[gi], v);
             } else {
                 out[gi] = v;
             }
@@ -466,25 +611,31 @@ paint_tile_kernel(PaintParams pp, const uint32_t *__restrict__ off,
 
 // ---- host side -----------------------------------------------------------------------------
 
-int paint_tiling_create(PaintTiling *t, int Ng, int tile) {
-    if (tile > kTileMax || tile < 5) tile = kTileMax;
-    int nt = (int)ceil_div(Ng, tile);
-    // with more than one tile per axis every extent must be >= 5 so that a
-    // stencil reaches at most the adjacent tile and the classes are exclusive
-    while (nt > 1 && Ng / nt < 5) --nt;
-    std::vector<int> tab(Ng + nt + 1);
-    int tmax = 0;
-    for (int a = 0; a <= nt; ++a) tab[Ng + a] = (int)((long)a * Ng / nt);
-    for (int a = 0; a < nt; ++a) {
-        const int s0 = tab[Ng + a], s1 = tab[Ng + a + 1];
-        tmax = s1 - s0 > tmax ? s1 - s0 : tmax;
-        for (int c = s0; c < s1; ++c) tab[c] = a;
+int paint_tiling_create(PaintTiling *t, int Ng) {
+    std::vector<int> tab;
+    long nk = 27;
+    for (int a = 0; a < 3; ++a) {
+        int nt = (int)ceil_div(Ng, kTileExt[a]);
+        // with more than one tile per axis every extent must be >= 5 so that a
+        // stencil reaches at most the adjacent tile and the classes are exclusive
+        while (nt > 1 && Ng / nt < 5) --nt;
+        t->tab_off[a] = (int)tab.size();
+        const size_t base = tab.size();
+        tab.resize(base + Ng + nt + 1);
+        int tmax = 0;
+        for (int q = 0; q <= nt; ++q) tab[base + Ng + q] = (int)((long)q * Ng / nt);
+        for (int q = 0; q < nt; ++q) {
+            const int s0 = tab[base + Ng + q], s1 = tab[base + Ng + q + 1];
+            tmax = s1 - s0 > tmax ? s1 - s0 : tmax;
+            for (int c = s0; c < s1; ++c) tab[base + c] = q;
+        }
+        if (tmax > kTileExt[a]) return set_error(ERR_STATE, "paint tile extent %d > %d", tmax, kTileExt[a]);
+        t->nt[a] = nt;
+        t->tmax[a] = tmax;
+        nk *= nt;
     }
-    if (tmax > kTileMax) return set_error(ERR_STATE, "paint tile extent %d > %d", tmax, kTileMax);
     t->Ng = Ng;
-    t->nt = nt;
-    t->tmax = tmax;
-    t->nkeys = (long)nt * nt * nt * 27;
+    t->nkeys = nk;
     if (t->nkeys >= (1L << 32)) return set_error(ERR_UNSUPPORTED, "too many paint tiles");
     FG_CUDA(cudaMalloc(&t->d_tables, sizeof(int) * tab.size()));
     FG_CUDA(cudaMemcpy(t->d_tables, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice));
@@ -526,8 +677,7 @@ static int ensure_scratch(PaintScratch *s, long Np, long nkeys) {
         FG_CUDA(cudaMalloc(&s->scan_tmp, sizeof(uint32_t) * (ceil_div(nkeys + 1, kScanBlock) + 1)));
         s->cap_keys = nkeys + 1;
     }
-    s->bytes = (sizeof(uint32_t) * 2 + 32) * (size_t)s->cap_particles +
-               sizeof(uint32_t) * (size_t)s->cap_keys;
+    s->bytes = (sizeof(uint32_t) * 2 + 32) * (size_t)s->cap_particles + sizeof(uint32_t) * (size_t)s->cap_keys;
     return OK;
 }
 
@@ -536,12 +686,11 @@ static void split(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 
-int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, const void *y,
-          const void *z, int pos_prec, long Np, double Hinv, const PaintGridSpec *grids,
-          int ngrids, cudaStream_t st, cudaEvent_t *ev) {
+int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, const void *y, const void *z,
+          int pos_prec, long Np, double Hinv, const PaintGridSpec *grids, int ngrids, cudaStream_t st,
+          cudaEvent_t *ev) {
     if (ngrids < 1 || ngrids > kMaxPaintGrids) return set_error(ERR_ARG, "paint: 1 or 2 grids");
-    if (pos_prec != grid_prec)
-        return set_error(ERR_ARG, "paint: position precision must match grid precision");
+    if (pos_prec != grid_prec) return set_error(ERR_ARG, "paint: position precision must match grid precision");
     if (Np < 0 || Np >= (1L << 32)) return set_error(ERR_ARG, "paint: Np out of range");
     for (int g = 1; g < ngrids; ++g)
         for (int a = 0; a < 3; ++a)
@@ -552,11 +701,11 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     memset(&pp, 0, sizeof(pp));
     pp.Ng = Ng;
     pp.Ng_pad = 2 * (Ng / 2 + 1);
-    pp.nt = t->nt;
     pp.ngrids = ngrids;
-    pp.tile_of = t->d_tables;
-    pp.start = t->d_tables + Ng;
     for (int a = 0; a < 3; ++a) {
+        pp.nt[a] = t->nt[a];
+        pp.tile_of[a] = t->d_tables + t->tab_off[a];
+        pp.start[a] = t->d_tables + t->tab_off[a] + Ng;
         split(Hinv, pp.ax[a].h_hi, pp.ax[a].h_lo);
         pp.ax[a].h = Hinv;
         for (int g = 0; g < ngrids; ++g) {
@@ -577,11 +726,11 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     const unsigned gp = (unsigned)(Np > 0 ? (ceil_div(Np, 256) < 32L * nsm ? ceil_div(Np, 256) : 32L * nsm) : 1);
     if (Np > 0) {
         if (pos_prec == 4)
-            paint_key_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y,
-                                                       (const float *)z, Np, pp, s->key, s->rank, s->hist);
+            paint_key_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z, Np,
+                                                       pp, s->key, s->rank, s->hist);
         else
-            paint_key_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y,
-                                                        (const double *)z, Np, pp, s->key, s->rank, s->hist);
+            paint_key_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y, (const double *)z,
+                                                        Np, pp, s->key, s->rank, s->hist);
         FG_LAUNCHED(1);
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[0], st));
@@ -589,28 +738,27 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (ev) FG_CUDA(cudaEventRecord(ev[1], st));
     if (Np > 0) {
         if (pos_prec == 4)
-            paint_scatter_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y,
-                                                           (const float *)z, Np, s->key, s->rank, s->hist,
-                                                           (float4 *)s->sorted);
+            paint_scatter_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z,
+                                                           Np, s->key, s->rank, s->hist, (float4 *)s->sorted);
         else
-            paint_scatter_kernel<double><<<gp, 256, 0, st>>>(
-                (const double *)x, (const double *)y, (const double *)z, Np, s->key, s->rank, s->hist,
-                (Rec<double>::type *)s->sorted);
+            paint_scatter_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y,
+                                                            (const double *)z, Np, s->key, s->rank, s->hist,
+                                                            (Rec<double>::type *)s->sorted);
         FG_LAUNCHED(1);
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
-    const unsigned ntiles = (unsigned)((long)t->nt * t->nt * t->nt);
-    const size_t smem = (size_t)ngrids * kTileMax * kTileMax * kTileMax * (grid_prec == 4 ? 4 : 8);
+    const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
-        FG_CUDA(cudaFuncSetAttribute(paint_tile_kernel<float>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        paint_tile_kernel<float><<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist,
-                                                                    (const float4 *)s->sorted, po);
+        const size_t smem = sizeof(uint32_t) * kMaxPaintGrids * kGS +
+                            sizeof(StageRec) * (kPaintThreads / 32) * 32 * kMaxPaintGrids + sizeof(uint32_t) * kBlkN;
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        paint_coop_kernel<<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist, (const float4 *)s->sorted, po);
     } else {
-        FG_CUDA(cudaFuncSetAttribute(paint_tile_kernel<double>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        paint_tile_kernel<double><<<ntiles, kPaintThreads, smem, st>>>(
-            pp, s->hist, (const Rec<double>::type *)s->sorted, po);
+        const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
+        FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        paint_tile_f64_kernel<<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist,
+                                                                    (const Rec<double>::type *)s->sorted, po);
     }
     FG_LAUNCHED(1);
     if (ev) FG_CUDA(cudaEventRecord(ev[3], st));

@@ -227,12 +227,48 @@ __global__ void finish_kernel(T *A, const T *__restrict__ B, int Ng, T H3, const
     }
 }
 
+// FP32: one warp per k row; the row's i and j factors are formed once and
+// the per-axis tables sit in shared memory as FP32
+__global__ void __launch_bounds__(256)
+finish_f32_kernel(float *A, const float *__restrict__ B, int Ng, float scale, const double *__restrict__ tab,
+                  const double *__restrict__ winv) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *ph = reinterpret_cast<float2 *>(smem_raw);  // [3][Ng]
+    float *w = reinterpret_cast<float *>(ph + 3 * Ng);   // [Ng]
+    for (int e = threadIdx.x; e < 3 * Ng; e += blockDim.x)
+        ph[e] = make_float2((float)tab[2 * e], (float)tab[2 * e + 1]);
+    for (int e = threadIdx.x; e < Ng; e += blockDim.x) w[e] = (float)winv[e];
+    __syncthreads();
+    const int nh = Ng / 2 + 1, lane = threadIdx.x & 31;
+    const int nwarp = blockDim.x >> 5;
+    const int nrows = Ng * Ng;
+    float2 *a = reinterpret_cast<float2 *>(A);
+    const float2 *b = reinterpret_cast<const float2 *>(B);
+    for (int row = blockIdx.x * nwarp + (threadIdx.x >> 5); row < nrows; row += gridDim.x * nwarp) {
+        const int i = row / Ng, j = row - i * Ng;
+        const float2 pij = cmul(ph[i], ph[Ng + j]);
+        const float wij = w[i] * w[j] * scale;
+        const long base = (long)row * nh;
+        for (int k = lane; k < nh; k += 32) {
+            const float2 p = cmul(pij, ph[2 * Ng + k]);
+            const float wk = wij * w[k];
+            const float2 bv = b[base + k], av = a[base + k];
+            const float2 dv = cmul(bv, p);
+            a[base + k] = make_float2((dv.x + av.x) * wk, (dv.y + av.y) * wk);
+        }
+    }
+}
+
 int interlace_finish(void *A, const void *B, int Ng, int prec, double H3, const void *d_tab,
                      const void *d_winv, cudaStream_t st) {
-    if (prec == 4)
-        finish_kernel<float><<<chunk_blocks(Ng), 256, 0, st>>>((float *)A, (const float *)B, Ng, (float)H3,
-                                                             (const double *)d_tab, (const double *)d_winv);
-    else
+    if (prec == 4) {
+        const size_t smem = sizeof(float2) * 3 * Ng + sizeof(float) * Ng;
+        FG_CUDA(cudaFuncSetAttribute(finish_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        long nb = ceil_div((long)Ng * Ng, 8);
+        if (nb > 8L * num_sms()) nb = 8L * num_sms();
+        finish_f32_kernel<<<(unsigned)nb, 256, smem, st>>>((float *)A, (const float *)B, Ng, (float)(0.5 * H3),
+                                                          (const double *)d_tab, (const double *)d_winv);
+    } else
         finish_kernel<double><<<chunk_blocks(Ng), 256, 0, st>>>((double *)A, (const double *)B, Ng, H3,
                                                               (const double *)d_tab, (const double *)d_winv);
     FG_LAUNCHED(1);
