@@ -418,7 +418,16 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     const uint32_t total = ts.total;
     const int nseg = ts.nseg;
 
-    // pass A: particles per 4^3 block of base cells (tile plus a 4-cell margin)
+    // pass A: particles per 4^3 block of grid-0 base cells.  Along an axis cut
+    // into several tiles the blocks cover the tile plus a 4-cell margin; along
+    // an axis held by a single tile they tile the periodic axis itself.
+    int nb[3];
+    bool cyc[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cyc[a] = ts.te[a] == Ng;
+        nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
+    }
     for (uint32_t q = tid; q < total; q += blockDim.x) {
         const float4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
         const float pos[3] = {r.x, r.y, r.z};
@@ -428,38 +437,47 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
             int b;
             float d;
             coord(pos[a], pp.ax[a], 0, Ng, b, d);
-            int l = b - ts.t0[a];
-            if (l > Ng / 2) l -= Ng;
-            if (l < -Ng / 2) l += Ng;
-            int bb = (l + 4) / kBlk;  // margin of 4 cells below the tile
-            bb = bb < 0 ? 0 : (bb >= blk_dim(a) ? blk_dim(a) - 1 : bb);
+            int bb;
+            if (cyc[a]) {
+                bb = b / kBlk;
+            } else {
+                int l = b - ts.t0[a];
+                if (l > Ng / 2) l -= Ng;
+                if (l < -Ng / 2) l += Ng;
+                bb = (l + 4) / kBlk;  // margin of 4 cells below the tile
+                bb = bb < 0 ? 0 : (bb >= nb[a] ? nb[a] - 1 : bb);
+            }
             bidx = bidx * blk_dim(a) + bb;
         }
         atomicAdd(&blk[bidx], 1u);
     }
     __syncthreads();
-    // a cell's contributors have grid-0 base cells within 3 below to 2 above
-    // it per axis: at most 3 consecutive blocks per axis
+    // A cell's contributors have grid-0 base cells from 3 below to 3 above it
+    // per axis, within 3 consecutive blocks (cyclically on a periodic axis):
+    // the largest 3x3x3 block sum bounds every cell's contributor count.
     if (tid < 32) {
         uint32_t mx = 0;
-        for (int e = lane; e < kBlkN; e += 32) {
-            const int bk = e % blk_dim(2), bj = (e / blk_dim(2)) % blk_dim(1), bi = e / (blk_dim(2) * blk_dim(1));
-            if (bi + 2 >= blk_dim(0) || bj + 2 >= blk_dim(1) || bk + 2 >= blk_dim(2)) continue;
-            uint32_t s = 0;
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b)
-                    for (int c = 0; c < 3; ++c) s += blk[((bi + a) * blk_dim(1) + bj + b) * blk_dim(2) + bk + c];
-            mx = max(mx, s);
+        const int w0 = cyc[0] ? nb[0] : nb[0] - 2, w1 = cyc[1] ? nb[1] : nb[1] - 2, w2 = cyc[2] ? nb[2] : nb[2] - 2;
+        for (int e = lane; e < w0 * w1 * w2; e += 32) {
+            const int sk = e % w2, sj = (e / w2) % w1, si = e / (w2 * w1);
+            uint32_t sum = 0;
+            for (int a = 0; a < 3; ++a) {
+                const int bi = cyc[0] ? (si + a) % nb[0] : si + a;
+                for (int b = 0; b < 3; ++b) {
+                    const int bj = cyc[1] ? (sj + b) % nb[1] : sj + b;
+                    for (int c = 0; c < 3; ++c) {
+                        const int bk = cyc[2] ? (sk + c) % nb[2] : sk + c;
+                        sum += blk[(bi * blk_dim(1) + bj) * blk_dim(2) + bk];
+                    }
+                }
+            }
+            mx = max(mx, sum);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if (lane == 0) {
-            // a tile of one axis-wrapping extent can see a particle twice per
-            // axis through the periodic images: bound by the total instead
-            const bool wraps = ts.te[0] == Ng || ts.te[1] == Ng || ts.te[2] == Ng;
-            const double cnt = wraps ? (double)total : (double)mx;
             int fb = 31;
-            if (cnt > 0) fb = (int)floor(log2(4294967295.0 / (cnt * kMaxCellWeight)));
+            if (mx > 0) fb = (int)floor(log2(4294967295.0 / ((double)mx * kMaxCellWeight)));
             fixbits_s = fb > 31 ? 31 : fb;
         }
     }
