@@ -88,6 +88,31 @@ __device__ __forceinline__ int wedge_index(int ki, int kj, int kk, float kamp, c
     return (int)t;
 }
 
+// the same with mu = num * rsqrt(n2) (a few ulp; the tie band of
+// wedge_index covers it)
+__device__ __forceinline__ int wedge_index_r(int ki, int kj, int kk, float rkamp, const BinDev &d, float &mu2) {
+    if (d.zero_los) {
+        mu2 = 0.f;
+        return 0;
+    }
+    const float num = (float)ki * d.l0f + (float)kj * d.l1f + (float)kk * d.l2f;
+    const float mu = num * rkamp;
+    mu2 = mu * mu;
+    const float t = fabsf(mu * (float)d.Nmu);
+    const float eps = 2e-6f * (float)(d.Nmu + 1);
+    const float r = rintf(t);
+    if (r >= 1.f && fabsf(t - r) < eps) return wedge_exact(ki, kj, kk, d);
+    return (int)t;
+}
+
+__device__ __forceinline__ int kbin_est(uint32_t n2, float kamp, const uint32_t *thr, int NK, float dKinv_f) {
+    int b = (int)(kamp * dKinv_f);
+    b = b < 0 ? 0 : (b > NK ? NK : b);
+    while (b > 0 && n2 < thr[b]) --b;
+    while (b < NK && n2 >= thr[b + 1]) ++b;
+    return b;
+}
+
 // ---- geometry: exact (n2, imu) multiplicities -----------------------------------------------
 __global__ void geometry_kernel(BinDev d, uint32_t *__restrict__ hist) {
     const long n = (long)d.Ng * d.Ng * d.nh;
@@ -384,7 +409,7 @@ bin_power_seg_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Ps
             const int ki = kval(i, Ng), kj = kval(j, Ng);
             const int n2ij = ki * ki + kj * kj;
             const float *frow = f + (long)row * Ng_pad;
-            int cb = -1, cw = -1;
+            int cb = -1, cm = -1;
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, sw = 0.f;
             const int k1 = min(nh, (seg + 1) * kSegModes);
             for (int k = seg * kSegModes; k < k1; ++k) {
@@ -398,31 +423,33 @@ bin_power_seg_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Ps
                     const float2 v = reinterpret_cast<const float2 *>(frow)[k];
                     p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
                 }
-                const float pc = (2 * k) % Ng > 0 ? 2.f * p : p;
-                int b = kbin(n2, thr, NK, d.dKinv_f);
+                const float pc = (k != 0 && 2 * k != Ng) ? 2.f * p : p;  // count 1 + (2k % Ng > 0)
+                const float n2f = (float)n2;
+                const float rk = rsqrtf(n2f);
+                int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
                 if (b >= NK) b = -1;
                 float m2;
-                const int imu = wedge_index(ki, kj, kk, sqrtf((float)n2), d, m2);
+                const int imu = wedge_index_r(ki, kj, kk, rk, d, m2);
                 if (b != cb) {
                     if (cb >= 0) {
                         atomicAdd(acc32 + 0 * NK + cb, s0);
                         atomicAdd(acc32 + 1 * NK + cb, s1);
                         atomicAdd(acc32 + 2 * NK + cb, s2);
                         atomicAdd(acc32 + 3 * NK + cb, s3);
+                        atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
                     }
                     cb = b;
-                    s0 = s1 = s2 = s3 = 0.f;
+                    cm = imu;
+                    s0 = s1 = s2 = s3 = sw = 0.f;
+                } else if (imu != cm) {
+                    if (cb >= 0) atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
+                    cm = imu;
+                    sw = 0.f;
                 }
                 s0 += pc;
                 s1 += pc * (1.5f * m2 - 0.5f);
                 s2 += pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f);
                 s3 += pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f);
-                const int wk = b < 0 ? -1 : b * W + imu;
-                if (wk != cw) {
-                    if (cw >= 0) atomicAdd(acc32 + (4 + cw % W) * NK + cw / W, sw);
-                    cw = wk;
-                    sw = 0.f;
-                }
                 sw += pc;
             }
             if (cb >= 0) {
@@ -430,8 +457,8 @@ bin_power_seg_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Ps
                 atomicAdd(acc32 + 1 * NK + cb, s1);
                 atomicAdd(acc32 + 2 * NK + cb, s2);
                 atomicAdd(acc32 + 3 * NK + cb, s3);
+                atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
             }
-            if (cw >= 0) atomicAdd(acc32 + (4 + cw % W) * NK + cw / W, sw);
         }
         __syncthreads();
         for (int e = tid; e < NK * NQ; e += blockDim.x) {

@@ -382,9 +382,9 @@ __device__ __forceinline__ uint32_t seg_index(uint32_t q, const uint32_t *seg_be
     return seg_begin[lo] + (q - seg_pref[lo]);
 }
 
-struct StageRec {
-    uint32_t loc[3];  // per axis: 4 packed local cell indices (255 = outside the tile)
-    float w[3][4];    // per axis: PCS weights
+struct __align__(16) StageRec {
+    uint32_t loc[4];  // per axis: 4 packed local cell indices (255 = outside the tile); [3] unused
+    float4 w[3];      // per axis: PCS weights (k weights pre-scaled by 2^s)
 };
 
 __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
@@ -411,7 +411,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
 
     const int Ng = pp.Ng, ngr = pp.ngrids;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    for (int e = tid; e < ngr * kGS; e += blockDim.x) acc[e] = 0u;
+    for (int e = tid; e < ngr * kGS / 4; e += blockDim.x) reinterpret_cast<uint4 *>(acc)[e] = make_uint4(0, 0, 0, 0);
     for (int e = tid; e < kBlkN; e += blockDim.x) blk[e] = 0u;
     TileSegs ts;
     tile_segments(pp, off, seg_begin, seg_pref, scan_ws, ts);
@@ -455,29 +455,47 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     // A cell's contributors have grid-0 base cells from 3 below to 3 above it
     // per axis, within 3 consecutive blocks (cyclically on a periodic axis):
     // the largest 3x3x3 block sum bounds every cell's contributor count.
-    if (tid < 32) {
+    // Separable window sums along k, then j, then i; tmp reuses the stage area.
+    {
+        uint32_t *tmp = reinterpret_cast<uint32_t *>(stage);
+        const int D1 = blk_dim(1), D2 = blk_dim(2);
+        for (int e = tid; e < kBlkN; e += blockDim.x) {
+            const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
+            uint32_t v = 0;
+            const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[2] || k + 2 < nb[2]);
+            if (in)
+                for (int c = 0; c < 3; ++c) v += blk[(i * D1 + j) * D2 + (cyc[2] ? (k + c) % nb[2] : k + c)];
+            tmp[e] = v;
+        }
+        __syncthreads();
+        for (int e = tid; e < kBlkN; e += blockDim.x) {
+            const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
+            uint32_t v = 0;
+            const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[1] || j + 2 < nb[1]);
+            if (in)
+                for (int c = 0; c < 3; ++c) v += tmp[(i * D1 + (cyc[1] ? (j + c) % nb[1] : j + c)) * D2 + k];
+            blk[e] = v;
+        }
+        __syncthreads();
         uint32_t mx = 0;
-        const int w0 = cyc[0] ? nb[0] : nb[0] - 2, w1 = cyc[1] ? nb[1] : nb[1] - 2, w2 = cyc[2] ? nb[2] : nb[2] - 2;
-        for (int e = lane; e < w0 * w1 * w2; e += 32) {
-            const int sk = e % w2, sj = (e / w2) % w1, si = e / (w2 * w1);
-            uint32_t sum = 0;
-            for (int a = 0; a < 3; ++a) {
-                const int bi = cyc[0] ? (si + a) % nb[0] : si + a;
-                for (int b = 0; b < 3; ++b) {
-                    const int bj = cyc[1] ? (sj + b) % nb[1] : sj + b;
-                    for (int c = 0; c < 3; ++c) {
-                        const int bk = cyc[2] ? (sk + c) % nb[2] : sk + c;
-                        sum += blk[(bi * blk_dim(1) + bj) * blk_dim(2) + bk];
-                    }
-                }
+        for (int e = tid; e < kBlkN; e += blockDim.x) {
+            const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
+            const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[0] || i + 2 < nb[0]);
+            if (in) {
+                uint32_t v = 0;
+                for (int c = 0; c < 3; ++c) v += blk[((cyc[0] ? (i + c) % nb[0] : i + c) * D1 + j) * D2 + k];
+                mx = max(mx, v);
             }
-            mx = max(mx, sum);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) {
+        if (lane == 0) scan_ws[warp] = mx;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t m = 0;
+            for (int w = 0; w < nwarp; ++w) m = max(m, scan_ws[w]);
             int fb = 31;
-            if (mx > 0) fb = (int)floor(log2(4294967295.0 / ((double)mx * kMaxCellWeight)));
+            if (m > 0) fb = (int)floor(log2(4294967295.0 / ((double)m * kMaxCellWeight)));
             fixbits_s = fb > 31 ? 31 : fb;
         }
     }
@@ -487,7 +505,6 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
 
     // pass B: stage 32 particles per warp, then deposit them one by one
-    const int g_l = lane >> 4, a_l = (lane >> 2) & 3, b_l = lane & 3;
     StageRec *mystage = stage + warp * 32 * kMaxPaintGrids;
     for (uint32_t base = (uint32_t)warp * 32; base < total; base += (uint32_t)nwarp * 32) {
         const uint32_t q = base + lane;
@@ -504,30 +521,53 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
                     float w[4];
                     pcs_weights(d, w);
                     st.loc[a] = pack_local(b, Ng, ts.t0[a], ts.te[a]);
-#pragma unroll
-                    for (int s = 0; s < 4; ++s) st.w[a][s] = w[s] * (a == 2 ? fscale : 1.f);
+                    const float sc = a == 2 ? fscale : 1.f;
+                    st.w[a] = make_float4(w[0] * sc, w[1] * sc, w[2] * sc, w[3] * sc);
                 }
             }
         }
         __syncwarp();
         const int np = min(32u, total - base);
-        if (g_l < ngr) {
-            for (int p = 0; p < np; ++p) {
-                const StageRec &st = mystage[p * kMaxPaintGrids + g_l];
-                const int li = (st.loc[0] >> (8 * a_l)) & 255, lj = (st.loc[1] >> (8 * b_l)) & 255;
-                if (li == 255 || lj == 255) continue;
-                const float wij = st.w[0][a_l] * st.w[1][b_l];
-                uint32_t *row = acc + g_l * kGS + li * kSI + lj * kSJ;
-                const uint32_t lk = st.loc[2];
+        // 4 particles per step: lane = (particle slot, grid, i row); each lane
+        // adds the 16 (j row, k cell) weights of its i row
+        for (int p0 = 0; p0 < np; p0 += 4) {
+            const int p = p0 + (lane >> 3);
+            const int g = (lane >> 2) & 1, a = lane & 3;
+            if (p >= np || g >= ngr) continue;
+            const StageRec &st = mystage[p * kMaxPaintGrids + g];
+            const uint4 loc = *reinterpret_cast<const uint4 *>(st.loc);
+            const int li = (loc.x >> (8 * a)) & 255;
+            if (li == 255) continue;
+            const float4 wxv = st.w[0], wy = st.w[1], wz = st.w[2];
+            const float wa = a == 0 ? wxv.x : (a == 1 ? wxv.y : (a == 2 ? wxv.z : wxv.w));
+            uint32_t *plane = acc + g * kGS + li * kSI;
+            const float wyv[4] = {wy.x, wy.y, wy.z, wy.w};
+            const float wzv[4] = {wz.x, wz.y, wz.z, wz.w};
+            const int lk0 = loc.z & 255;
+            const bool kfull = ((loc.z & 0x80808080u) == 0) && (int)((loc.z >> 24) & 255) == lk0 + 3;
 #pragma unroll
-                for (int s = 0; s < 4; ++s) {
-                    const uint32_t l = (lk >> (8 * s)) & 255;
-                    if (l == 255) continue;
-                    const float wv = wij * st.w[2][s];
-                    if (fixed)
-                        atomicAdd(row + l, __float2uint_rn(wv));
-                    else
-                        atomicAdd(reinterpret_cast<float *>(row + l), wv);
+            for (int b = 0; b < 4; ++b) {
+                const int lj = (loc.y >> (8 * b)) & 255;
+                if (lj == 255) continue;
+                const float wab = wa * wyv[b];
+                uint32_t *row = plane + lj * kSJ;
+                if (fixed) {
+                    if (kfull) {
+#pragma unroll
+                        for (int s = 0; s < 4; ++s) atomicAdd(row + lk0 + s, __float2uint_rn(wab * wzv[s]));
+                    } else {
+#pragma unroll
+                        for (int s = 0; s < 4; ++s) {
+                            const int lk = (loc.z >> (8 * s)) & 255;
+                            if (lk != 255) atomicAdd(row + lk, __float2uint_rn(wab * wzv[s]));
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int s = 0; s < 4; ++s) {
+                        const int lk = (loc.z >> (8 * s)) & 255;
+                        if (lk != 255) atomicAdd(reinterpret_cast<float *>(row + lk), wab * wzv[s]);
+                    }
                 }
             }
         }
@@ -535,27 +575,31 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     }
     __syncthreads();
 
-    // write the owned cells (and the row padding of the last k tile)
+    // write the owned cells (and the row padding of the last k tile): one
+    // warp per (i, j) row, lanes along k
     const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
     const int pad = last_k ? pp.Ng_pad - Ng : 0;
     const int rowlen = ts.te[2] + pad;
-    const int ncell = ts.te[0] * ts.te[1] * rowlen;
+    const int nrow = ts.te[0] * ts.te[1];
     for (int g = 0; g < ngr; ++g) {
         float *out = reinterpret_cast<float *>(po.out[g]);
         const float sc = (float)ldexp(po.scale[g], fixed ? -fixbits : 0);
         const int accu = po.accumulate[g];
-        for (int e = tid; e < ncell; e += blockDim.x) {
-            const int lk = e % rowlen, lj = (e / rowlen) % ts.te[1], li = e / (rowlen * ts.te[1]);
-            const long gi = ((long)(ts.t0[0] + li) * Ng + (ts.t0[1] + lj)) * pp.Ng_pad + ts.t0[2] + lk;
-            float v = 0.f;
-            if (lk < ts.te[2]) {
-                const uint32_t a = acc[g * kGS + li * kSI + lj * kSJ + lk];
-                v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
-            }
-            if (accu) {
-                if (lk < ts.te[2]) out[gi] += v;
-            } else {
-                out[gi] = v;
+        for (int r = warp; r < nrow; r += nwarp) {
+            const int li = r / ts.te[1], lj = r - li * ts.te[1];
+            float *orow = out + ((long)(ts.t0[0] + li) * Ng + (ts.t0[1] + lj)) * pp.Ng_pad + ts.t0[2];
+            const uint32_t *arow = acc + g * kGS + li * kSI + lj * kSJ;
+            for (int lk = lane; lk < rowlen; lk += 32) {
+                float v = 0.f;
+                if (lk < ts.te[2]) {
+                    const uint32_t a = arow[lk];
+                    v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
+                }
+                if (accu) {
+                    if (lk < ts.te[2]) orow[lk] += v;
+                } else {
+                    orow[lk] = v;
+                }
             }
         }
     }
