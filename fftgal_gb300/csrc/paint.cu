@@ -293,7 +293,8 @@ __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restric
 
 // ---- 4. tile paint ---------------------------------------------------------------------
 
-constexpr int kPaintThreads = 256;
+constexpr int kPaintThreads = 512;
+constexpr int kStageParts = 16;  // particles staged per warp and round
 constexpr int kMaxSeg = 125;
 
 struct PaintOut {
@@ -388,11 +389,14 @@ struct __align__(16) StageRec {
 };
 
 __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
+    int c = b - 1;
+    c += c < 0 ? Ng : 0;
     uint32_t r = 0;
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        const int l = local_cell(b, s, Ng, t0, te);
-        r |= (uint32_t)(l < 0 ? 255 : l) << (8 * s);
+        const int cs = c + s - (c + s >= Ng ? Ng : 0);
+        const int l = cs - t0;
+        r |= (uint32_t)((unsigned)l < (unsigned)te ? l : 255) << (8 * s);
     }
     return r;
 }
@@ -403,7 +407,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS]
     StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS);  // [warps][32][grids]
-    uint32_t *blk = reinterpret_cast<uint32_t *>(stage + (kPaintThreads / 32) * 32 * kMaxPaintGrids);  // [kBlkN]
+    uint32_t *blk = reinterpret_cast<uint32_t *>(stage + (kPaintThreads / 32) * kStageParts * kMaxPaintGrids);  // [kBlkN]
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
     __shared__ uint32_t scan_ws[32];
@@ -505,10 +509,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
 
     // pass B: stage 32 particles per warp, then deposit them one by one
-    StageRec *mystage = stage + warp * 32 * kMaxPaintGrids;
-    for (uint32_t base = (uint32_t)warp * 32; base < total; base += (uint32_t)nwarp * 32) {
+    StageRec *mystage = stage + warp * kStageParts * kMaxPaintGrids;
+    for (uint32_t base = (uint32_t)warp * kStageParts; base < total; base += (uint32_t)nwarp * kStageParts) {
         const uint32_t q = base + lane;
-        if (q < total) {
+        if (lane < kStageParts && q < total) {
             const float4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
             const float pos[3] = {r.x, r.y, r.z};
             for (int g = 0; g < ngr; ++g) {
@@ -527,7 +531,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
             }
         }
         __syncwarp();
-        const int np = min(32u, total - base);
+        const int np = min((uint32_t)kStageParts, total - base);
         // 4 particles per step: lane = (particle slot, grid, i row); each lane
         // adds the 16 (j row, k cell) weights of its i row
         for (int p0 = 0; p0 < np; p0 += 4) {
@@ -812,7 +816,8 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
         const size_t smem = sizeof(uint32_t) * kMaxPaintGrids * kGS +
-                            sizeof(StageRec) * (kPaintThreads / 32) * 32 * kMaxPaintGrids + sizeof(uint32_t) * kBlkN;
+                            sizeof(StageRec) * (kPaintThreads / 32) * kStageParts * kMaxPaintGrids +
+                            sizeof(uint32_t) * kBlkN;
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         paint_coop_kernel<<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist, (const float4 *)s->sorted, po);
     } else {
