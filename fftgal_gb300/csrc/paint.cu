@@ -389,12 +389,12 @@ struct __align__(16) StageRec {
 };
 
 __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
-    int c = b - 1;
-    c += c < 0 ? Ng : 0;
     uint32_t r = 0;
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        const int cs = c + s - (c + s >= Ng ? Ng : 0);
+        int cs = b - 1 + s;  // in [-1, Ng + 2): one correction each way (Ng >= 2)
+        cs += cs < 0 ? Ng : 0;
+        cs -= cs >= Ng ? Ng : 0;
         const int l = cs - t0;
         r |= (uint32_t)((unsigned)l < (unsigned)te ? l : 255) << (8 * s);
     }
