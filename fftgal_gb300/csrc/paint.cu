@@ -58,6 +58,8 @@ struct AxisParams {
     // FP32 path: x * h - o as double-float (h = Ng/L, o = offset of grid g)
     float h_hi, h_lo;
     float o_hi[kMaxPaintGrids], o_lo[kMaxPaintGrids];
+    // FP32 path: u_g = u_0 + delta_g, delta_g = o_0 - o_g in units of 2^-fb
+    int dq[kMaxPaintGrids];
     // FP64 path
     double h;
     double o[kMaxPaintGrids];
@@ -66,6 +68,7 @@ struct AxisParams {
 struct PaintParams {
     AxisParams ax[3];
     int Ng, Ng_pad, ngrids;
+    int fb;                  // FP32 path: fraction bits of the packed cell coordinate
     int nt[3];
     const int *tile_of[3];   // [Ng] per axis
     const int *start[3];     // [nt + 1] per axis
@@ -127,6 +130,25 @@ __device__ __forceinline__ void pcs_weights(double d, double w[4]) {
     w[3] = __ddiv_rn(__dmul_rn(d2, d), 6.0);
 }
 
+// FP32 path: the grid-0 base cell b0 and the fraction as fb-bit fixed point;
+// every other grid's cell is derived from these with an exact integer shift,
+// identically in the key and the paint kernels.
+__device__ __forceinline__ void cell0(float x, const AxisParams &a, int Ng, int fb, int &b0, uint32_t &dq) {
+    float d;
+    coord(x, a, 0, Ng, b0, d);
+    const uint32_t one = 1u << fb;
+    dq = (uint32_t)(d * (float)one);
+    dq = dq >= one ? one - 1 : dq;
+}
+
+__device__ __forceinline__ void cell_g(int b0, uint32_t dq, int delta, int fb, int Ng, int &bg, uint32_t &dgq) {
+    const int t = (int)dq + delta;  // |delta| <= 2^fb
+    dgq = (uint32_t)t & ((1u << fb) - 1);
+    bg = b0 + (t >> fb);            // arithmetic shift: floor division
+    bg += bg < 0 ? Ng : 0;
+    bg -= bg >= Ng ? Ng : 0;
+}
+
 // local index of stencil cell s (0..3) of base cell b: (b - 1 + s) mod Ng
 // relative to the tile start t0, or -1 outside [0, te)
 __device__ __forceinline__ int local_cell(int b, int s, int Ng, int t0, int te) {
@@ -137,7 +159,7 @@ __device__ __forceinline__ int local_cell(int b, int s, int Ng, int t0, int te) 
 }
 
 template <typename P> struct Rec;
-template <> struct Rec<float> { using type = float4; };
+template <> struct Rec<float> { using type = uint4; };  // per axis (b0 << fb) | fraction
 template <> struct Rec<double> { struct type { double x, y, z; }; };
 
 // ---- 1. key + histogram -------------------------------------------------------
@@ -155,16 +177,26 @@ __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ 
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             int b0;
-            P d;
-            coord(pos[a], pp.ax[a], 0, Ng, b0, d);
+            uint32_t dq0 = 0;
+            if constexpr (sizeof(P) == 4) {
+                cell0(pos[a], pp.ax[a], Ng, pp.fb, b0, dq0);
+            } else {
+                P d;
+                coord(pos[a], pp.ax[a], 0, Ng, b0, d);
+            }
             const int ta = pp.tile_of[a][b0];
             const int t0 = pp.start[a][ta];
             const int te = pp.start[a][ta + 1] - t0;
             int rmin = b0 - t0, rmax = b0 - t0;
             for (int g = 1; g < pp.ngrids; ++g) {
                 int bg;
-                P dg;
-                coord(pos[a], pp.ax[a], g, Ng, bg, dg);
+                if constexpr (sizeof(P) == 4) {
+                    uint32_t dgq;
+                    cell_g(b0, dq0, pp.ax[a].dq[g], pp.fb, Ng, bg, dgq);
+                } else {
+                    P dg;
+                    coord(pos[a], pp.ax[a], g, Ng, bg, dg);
+                }
                 const int dl = ((bg - b0 + Ng + 1) % Ng) - 1;  // -1, 0 or +1
                 rmin = min(rmin, b0 - t0 + dl);
                 rmax = max(rmax, b0 - t0 + dl);
@@ -271,7 +303,7 @@ static int exclusive_scan(uint32_t *a, long n, uint32_t *bsum, cudaStream_t st) 
 
 template <typename P>
 __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restrict__ y,
-                                     const P *__restrict__ z, long Np,
+                                     const P *__restrict__ z, long Np, PaintParams pp,
                                      const uint32_t *__restrict__ key,
                                      const uint32_t *__restrict__ rank,
                                      const uint32_t *__restrict__ off,
@@ -281,7 +313,16 @@ __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restric
         const uint32_t dst = off[key[p]] + rank[p];
         typename Rec<P>::type r;
         if constexpr (sizeof(P) == 4) {
-            r = make_float4(x[p], y[p], z[p], 0.f);
+            const float pos[3] = {x[p], y[p], z[p]};
+            uint32_t w[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                int b0;
+                uint32_t dq;
+                cell0(pos[a], pp.ax[a], pp.Ng, pp.fb, b0, dq);
+                w[a] = ((uint32_t)b0 << pp.fb) | dq;
+            }
+            r = make_uint4(w[0], w[1], w[2], 0u);
         } else {
             r.x = x[p];
             r.y = y[p];
@@ -402,7 +443,7 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
 }
 
 __global__ void __launch_bounds__(kPaintThreads, 2)
-paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4 *__restrict__ sorted,
+paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS]
@@ -432,15 +473,14 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
         cyc[a] = ts.te[a] == Ng;
         nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
     }
+    const int fb = pp.fb;
     for (uint32_t q = tid; q < total; q += blockDim.x) {
-        const float4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
-        const float pos[3] = {r.x, r.y, r.z};
+        const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+        const uint32_t rw[3] = {r.x, r.y, r.z};
         int bidx = 0;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            int b;
-            float d;
-            coord(pos[a], pp.ax[a], 0, Ng, b, d);
+            const int b = (int)(rw[a] >> fb);
             int bb;
             if (cyc[a]) {
                 bb = b / kBlk;
@@ -511,23 +551,37 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
     // pass B: stage 32 particles per warp, then deposit them one by one
     StageRec *mystage = stage + warp * kStageParts * kMaxPaintGrids;
     for (uint32_t base = (uint32_t)warp * kStageParts; base < total; base += (uint32_t)nwarp * kStageParts) {
-        const uint32_t q = base + lane;
-        if (lane < kStageParts && q < total) {
-            const float4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
-            const float pos[3] = {r.x, r.y, r.z};
-            for (int g = 0; g < ngr; ++g) {
-                StageRec &st = mystage[lane * kMaxPaintGrids + g];
+        const uint32_t q = base + (lane & (kStageParts - 1));
+        const int gs = lane / kStageParts;  // lanes 0..15 stage grid 0, 16..31 grid 1
+        if (q < total && gs < ngr) {
+            const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+            const uint32_t rw[3] = {r.x, r.y, r.z};
+            StageRec &st = mystage[(lane & (kStageParts - 1)) * kMaxPaintGrids + gs];
+            const float inv = ldexpf(1.0f, -fb);
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    int b;
-                    float d;
-                    coord(pos[a], pp.ax[a], g, Ng, b, d);
-                    float w[4];
-                    pcs_weights(d, w);
-                    st.loc[a] = pack_local(b, Ng, ts.t0[a], ts.te[a]);
-                    const float sc = a == 2 ? fscale : 1.f;
-                    st.w[a] = make_float4(w[0] * sc, w[1] * sc, w[2] * sc, w[3] * sc);
+            for (int a = 0; a < 3; ++a) {
+                int bg;
+                uint32_t dgq;
+                cell_g((int)(rw[a] >> fb), rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
+                float w[4];
+                pcs_weights((float)dgq * inv, w);
+                uint32_t loc;
+                if (cyc[a]) {
+                    loc = pack_local(bg, Ng, ts.t0[a], ts.te[a]);
+                } else {
+                    // linear local index of the first stencil cell (periodic
+                    // images folded to the nearest copy of the tile)
+                    int l = bg - 1 - ts.t0[a];
+                    l -= l > Ng / 2 ? Ng : 0;
+                    l += l < -Ng / 2 ? Ng : 0;
+                    loc = 0;
+#pragma unroll
+                    for (int s4 = 0; s4 < 4; ++s4)
+                        loc |= (uint32_t)((unsigned)(l + s4) < (unsigned)ts.te[a] ? l + s4 : 255) << (8 * s4);
                 }
+                st.loc[a] = loc;
+                const float sc = a == 2 ? fscale : 1.f;
+                st.w[a] = make_float4(w[0] * sc, w[1] * sc, w[2] * sc, w[3] * sc);
             }
         }
         __syncwarp();
@@ -547,31 +601,21 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const float4
             uint32_t *plane = acc + g * kGS + li * kSI;
             const float wyv[4] = {wy.x, wy.y, wy.z, wy.w};
             const float wzv[4] = {wz.x, wz.y, wz.z, wz.w};
-            const int lk0 = loc.z & 255;
-            const bool kfull = ((loc.z & 0x80808080u) == 0) && (int)((loc.z >> 24) & 255) == lk0 + 3;
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const int lj = (loc.y >> (8 * b)) & 255;
                 if (lj == 255) continue;
                 const float wab = wa * wyv[b];
                 uint32_t *row = plane + lj * kSJ;
-                if (fixed) {
-                    if (kfull) {
 #pragma unroll
-                        for (int s = 0; s < 4; ++s) atomicAdd(row + lk0 + s, __float2uint_rn(wab * wzv[s]));
-                    } else {
-#pragma unroll
-                        for (int s = 0; s < 4; ++s) {
-                            const int lk = (loc.z >> (8 * s)) & 255;
-                            if (lk != 255) atomicAdd(row + lk, __float2uint_rn(wab * wzv[s]));
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int s = 0; s < 4; ++s) {
-                        const int lk = (loc.z >> (8 * s)) & 255;
-                        if (lk != 255) atomicAdd(reinterpret_cast<float *>(row + lk), wab * wzv[s]);
-                    }
+                for (int s4 = 0; s4 < 4; ++s4) {
+                    const uint32_t lk = (loc.z >> (8 * s4)) & 255;
+                    if (lk == 255) continue;
+                    const float wv = wab * wzv[s4];
+                    if (fixed)
+                        atomicAdd(row + lk, __float2uint_rn(wv));
+                    else
+                        atomicAdd(reinterpret_cast<float *>(row + lk), wv);
                 }
             }
         }
@@ -768,6 +812,10 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     pp.Ng = Ng;
     pp.Ng_pad = 2 * (Ng / 2 + 1);
     pp.ngrids = ngrids;
+    int bits_b = 1;
+    while ((1 << bits_b) < Ng) ++bits_b;
+    pp.fb = 32 - bits_b < 24 ? 32 - bits_b : 24;  // 2^-24 cell: below FP32 resolution
+    if (grid_prec == 4 && pp.fb < 16) return set_error(ERR_UNSUPPORTED, "FP32 paint: Ng=%d too large", Ng);
     for (int a = 0; a < 3; ++a) {
         pp.nt[a] = t->nt[a];
         pp.tile_of[a] = t->d_tables + t->tab_off[a];
@@ -777,6 +825,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
         for (int g = 0; g < ngrids; ++g) {
             split(grids[g].offset[a], pp.ax[a].o_hi[g], pp.ax[a].o_lo[g]);
             pp.ax[a].o[g] = grids[g].offset[a];
+            pp.ax[a].dq[g] = (int)llrint((grids[0].offset[a] - grids[g].offset[a]) * (double)(1u << pp.fb));
         }
     }
     PaintOut po;
@@ -805,10 +854,10 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (Np > 0) {
         if (pos_prec == 4)
             paint_scatter_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z,
-                                                           Np, s->key, s->rank, s->hist, (float4 *)s->sorted);
+                                                           Np, pp, s->key, s->rank, s->hist, (uint4 *)s->sorted);
         else
             paint_scatter_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y,
-                                                            (const double *)z, Np, s->key, s->rank, s->hist,
+                                                            (const double *)z, Np, pp, s->key, s->rank, s->hist,
                                                             (Rec<double>::type *)s->sorted);
         FG_LAUNCHED(1);
     }
@@ -819,7 +868,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
                             sizeof(StageRec) * (kPaintThreads / 32) * kStageParts * kMaxPaintGrids +
                             sizeof(uint32_t) * kBlkN;
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        paint_coop_kernel<<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist, (const float4 *)s->sorted, po);
+        paint_coop_kernel<<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po);
     } else {
         const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
         FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
