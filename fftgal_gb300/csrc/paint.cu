@@ -442,6 +442,45 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
     return r;
 }
 
+// deposit 4 staged particles: lane = (particle slot, grid, i row); every lane
+// adds its i row's 16 (j, k) cells, predicated on the packed validity bytes
+template <bool FIXED>
+__device__ __forceinline__ void deposit4(uint32_t *acc, const StageRec *mystage, int p0, int np, int ngr,
+                                         int lane) {
+    const int p = p0 + (lane >> 3);
+    const int g = (lane >> 2) & 1, a = lane & 3;
+    if (p >= np || g >= ngr) return;
+    const StageRec &st = mystage[p * kMaxPaintGrids + g];
+    const uint4 loc = *reinterpret_cast<const uint4 *>(st.loc);
+    const uint32_t li = (loc.x >> (8 * a)) & 255u;
+    if (li == 255u) return;
+    const float4 wxv = st.w[0], wy = st.w[1], wz = st.w[2];
+    const float wa = a == 0 ? wxv.x : (a == 1 ? wxv.y : (a == 2 ? wxv.z : wxv.w));
+    uint32_t *plane = acc + g * kGS + li * kSI;
+    const uint32_t lk0 = loc.z & 255u, lk1 = (loc.z >> 8) & 255u, lk2 = (loc.z >> 16) & 255u, lk3 = loc.z >> 24;
+    const uint32_t lj0 = loc.y & 255u, lj1 = (loc.y >> 8) & 255u, lj2 = (loc.y >> 16) & 255u, lj3 = loc.y >> 24;
+    const float wab[4] = {wa * wy.x, wa * wy.y, wa * wy.z, wa * wy.w};
+    const uint32_t ljs[4] = {lj0, lj1, lj2, lj3};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const bool jok = ljs[b] != 255u;
+        uint32_t *row = plane + ljs[b] * kSJ;
+        const float w = wab[b];
+        if (FIXED) {
+            if (jok && lk0 != 255u) atomicAdd(row + lk0, __float2uint_rn(w * wz.x));
+            if (jok && lk1 != 255u) atomicAdd(row + lk1, __float2uint_rn(w * wz.y));
+            if (jok && lk2 != 255u) atomicAdd(row + lk2, __float2uint_rn(w * wz.z));
+            if (jok && lk3 != 255u) atomicAdd(row + lk3, __float2uint_rn(w * wz.w));
+        } else {
+            float *rowf = reinterpret_cast<float *>(row);
+            if (jok && lk0 != 255u) atomicAdd(rowf + lk0, w * wz.x);
+            if (jok && lk1 != 255u) atomicAdd(rowf + lk1, w * wz.y);
+            if (jok && lk2 != 255u) atomicAdd(rowf + lk2, w * wz.z);
+            if (jok && lk3 != 255u) atomicAdd(rowf + lk3, w * wz.w);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kPaintThreads, 2)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po) {
@@ -586,39 +625,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         }
         __syncwarp();
         const int np = min((uint32_t)kStageParts, total - base);
-        // 4 particles per step: lane = (particle slot, grid, i row); each lane
-        // adds the 16 (j row, k cell) weights of its i row
-        for (int p0 = 0; p0 < np; p0 += 4) {
-            const int p = p0 + (lane >> 3);
-            const int g = (lane >> 2) & 1, a = lane & 3;
-            if (p >= np || g >= ngr) continue;
-            const StageRec &st = mystage[p * kMaxPaintGrids + g];
-            const uint4 loc = *reinterpret_cast<const uint4 *>(st.loc);
-            const int li = (loc.x >> (8 * a)) & 255;
-            if (li == 255) continue;
-            const float4 wxv = st.w[0], wy = st.w[1], wz = st.w[2];
-            const float wa = a == 0 ? wxv.x : (a == 1 ? wxv.y : (a == 2 ? wxv.z : wxv.w));
-            uint32_t *plane = acc + g * kGS + li * kSI;
-            const float wyv[4] = {wy.x, wy.y, wy.z, wy.w};
-            const float wzv[4] = {wz.x, wz.y, wz.z, wz.w};
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int lj = (loc.y >> (8 * b)) & 255;
-                if (lj == 255) continue;
-                const float wab = wa * wyv[b];
-                uint32_t *row = plane + lj * kSJ;
-#pragma unroll
-                for (int s4 = 0; s4 < 4; ++s4) {
-                    const uint32_t lk = (loc.z >> (8 * s4)) & 255;
-                    if (lk == 255) continue;
-                    const float wv = wab * wzv[s4];
-                    if (fixed)
-                        atomicAdd(row + lk, __float2uint_rn(wv));
-                    else
-                        atomicAdd(reinterpret_cast<float *>(row + lk), wv);
-                }
-            }
-        }
+        if (fixed)
+            for (int p0 = 0; p0 < np; p0 += 4) deposit4<true>(acc, mystage, p0, np, ngr, lane);
+        else
+            for (int p0 = 0; p0 < np; p0 += 4) deposit4<false>(acc, mystage, p0, np, ngr, lane);
         __syncwarp();
     }
     __syncthreads();
