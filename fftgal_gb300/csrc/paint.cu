@@ -46,6 +46,8 @@ constexpr int kMinFixBits = 8;                 // below this: FP32 accumulation
 // kSJ = 1, kSI = 4, kGS = 16 (mod 32) gives the 32 rows (g, li+a, lj+b),
 // a, b < 4, of one stencil 32 distinct banks.
 constexpr int kSJ = 33, kSI = 548, kGS = 8784;
+// invalid (outside-tile) updates go to 32 per-lane trash words after the grids
+constexpr int kTrash = kMaxPaintGrids * kGS;
 static_assert(15 * kSI + 15 * kSJ + 31 < kGS, "tile does not fit the layout");
 // FP64 shared layout: dense [16][16][32]
 constexpr int kT3 = 16 * 16 * 32;
@@ -456,27 +458,27 @@ __device__ __forceinline__ void deposit4(uint32_t *acc, const StageRec *mystage,
     if (li == 255u) return;
     const float4 wxv = st.w[0], wy = st.w[1], wz = st.w[2];
     const float wa = a == 0 ? wxv.x : (a == 1 ? wxv.y : (a == 2 ? wxv.z : wxv.w));
-    uint32_t *plane = acc + g * kGS + li * kSI;
-    const uint32_t lk0 = loc.z & 255u, lk1 = (loc.z >> 8) & 255u, lk2 = (loc.z >> 16) & 255u, lk3 = loc.z >> 24;
-    const uint32_t lj0 = loc.y & 255u, lj1 = (loc.y >> 8) & 255u, lj2 = (loc.y >> 16) & 255u, lj3 = loc.y >> 24;
-    const float wab[4] = {wa * wy.x, wa * wy.y, wa * wy.z, wa * wy.w};
-    const uint32_t ljs[4] = {lj0, lj1, lj2, lj3};
+    // every update is issued: cells outside the tile go to this lane's trash
+    // word, so the 16 atomics run without branches
+    const uint32_t trash = kTrash + lane;
+    const uint32_t plane = g * kGS + li * kSI;
+    uint32_t koff[4];
+#pragma unroll
+    for (int s4 = 0; s4 < 4; ++s4) koff[s4] = (loc.z >> (8 * s4)) & 255u;
+    const float wyv[4] = {wy.x, wy.y, wy.z, wy.w};
+    const float wzv[4] = {wz.x, wz.y, wz.z, wz.w};
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const bool jok = ljs[b] != 255u;
-        uint32_t *row = plane + ljs[b] * kSJ;
-        const float w = wab[b];
-        if (FIXED) {
-            if (jok && lk0 != 255u) atomicAdd(row + lk0, __float2uint_rn(w * wz.x));
-            if (jok && lk1 != 255u) atomicAdd(row + lk1, __float2uint_rn(w * wz.y));
-            if (jok && lk2 != 255u) atomicAdd(row + lk2, __float2uint_rn(w * wz.z));
-            if (jok && lk3 != 255u) atomicAdd(row + lk3, __float2uint_rn(w * wz.w));
-        } else {
-            float *rowf = reinterpret_cast<float *>(row);
-            if (jok && lk0 != 255u) atomicAdd(rowf + lk0, w * wz.x);
-            if (jok && lk1 != 255u) atomicAdd(rowf + lk1, w * wz.y);
-            if (jok && lk2 != 255u) atomicAdd(rowf + lk2, w * wz.z);
-            if (jok && lk3 != 255u) atomicAdd(rowf + lk3, w * wz.w);
+        const uint32_t lj = (loc.y >> (8 * b)) & 255u;
+        const uint32_t row = plane + lj * kSJ;
+        const float w = wa * wyv[b];
+#pragma unroll
+        for (int s4 = 0; s4 < 4; ++s4) {
+            const uint32_t idx = (lj == 255u || koff[s4] == 255u) ? trash : row + koff[s4];
+            if (FIXED)
+                atomicAdd(acc + idx, __float2uint_rn(w * wzv[s4]));
+            else
+                atomicAdd(reinterpret_cast<float *>(acc) + idx, w * wzv[s4]);
         }
     }
 }
@@ -485,8 +487,8 @@ __global__ void __launch_bounds__(kPaintThreads, 2)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS]
-    StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS);  // [warps][32][grids]
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS] + trash[32]
+    StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS + 32);  // [warps][16][grids]
     uint32_t *blk = reinterpret_cast<uint32_t *>(stage + (kPaintThreads / 32) * kStageParts * kMaxPaintGrids);  // [kBlkN]
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
@@ -634,30 +636,37 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     __syncthreads();
 
     // write the owned cells (and the row padding of the last k tile): one
-    // warp per (i, j) row, lanes along k
+    // warp per (i, j) row, lanes along k, rows advanced incrementally
     const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
     const int pad = last_k ? pp.Ng_pad - Ng : 0;
-    const int rowlen = ts.te[2] + pad;
-    const int nrow = ts.te[0] * ts.te[1];
+    const int rowlen = ts.te[2] + pad, te1 = ts.te[1], te2 = ts.te[2];
+    const int nrow = ts.te[0] * te1;
+    const long rstride = (long)pp.Ng_pad;  // global floats between consecutive j
     for (int g = 0; g < ngr; ++g) {
-        float *out = reinterpret_cast<float *>(po.out[g]);
+        float *out = reinterpret_cast<float *>(po.out[g]) + ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
         const float sc = (float)ldexp(po.scale[g], fixed ? -fixbits : 0);
-        const int accu = po.accumulate[g];
+        const bool accu = po.accumulate[g] != 0;
+        int li = warp / te1, lj = warp - li * te1;
+        const int dli = nwarp / te1, dlj = nwarp - dli * te1;
         for (int r = warp; r < nrow; r += nwarp) {
-            const int li = r / ts.te[1], lj = r - li * ts.te[1];
-            float *orow = out + ((long)(ts.t0[0] + li) * Ng + (ts.t0[1] + lj)) * pp.Ng_pad + ts.t0[2];
+            float *orow = out + ((long)li * Ng + lj) * rstride;
             const uint32_t *arow = acc + g * kGS + li * kSI + lj * kSJ;
             for (int lk = lane; lk < rowlen; lk += 32) {
                 float v = 0.f;
-                if (lk < ts.te[2]) {
+                if (lk < te2) {
                     const uint32_t a = arow[lk];
                     v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
                 }
-                if (accu) {
-                    if (lk < ts.te[2]) orow[lk] += v;
-                } else {
+                if (!accu)
                     orow[lk] = v;
-                }
+                else if (lk < te2)
+                    orow[lk] += v;
+            }
+            li += dli;
+            lj += dlj;
+            if (lj >= te1) {
+                lj -= te1;
+                ++li;
             }
         }
     }
@@ -874,7 +883,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
-        const size_t smem = sizeof(uint32_t) * kMaxPaintGrids * kGS +
+        const size_t smem = sizeof(uint32_t) * (kMaxPaintGrids * kGS + 32) +
                             sizeof(StageRec) * (kPaintThreads / 32) * kStageParts * kMaxPaintGrids +
                             sizeof(uint32_t) * kBlkN;
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
