@@ -44,11 +44,16 @@ constexpr double kMaxCellWeight = 8.0 / 27.0;  // largest PCS weight product
 constexpr int kMinFixBits = 8;                 // below this: FP32 accumulation
 // FP32 shared layout: cell (li, lj, lk) of grid g at g*kGS + li*kSI + lj*kSJ + lk;
 // kSJ = 1, kSI = 4, kGS = 16 (mod 32) gives the 32 rows (g, li+a, lj+b),
-// a, b < 4, of one stencil 32 distinct banks.
-constexpr int kSJ = 33, kSI = 548, kGS = 8784;
-// invalid (outside-tile) updates go to 32 per-lane trash words after the grids
-constexpr int kTrash = kMaxPaintGrids * kGS;
-static_assert(15 * kSI + 15 * kSJ + 31 < kGS, "tile does not fit the layout");
+// a, b < 4, of one stencil 32 distinct banks.  Row lj = 16 and column lk = 32
+// are padding that absorbs the updates of stencil cells outside the tile, so
+// the deposit needs no per-cell test.
+constexpr int kSJ = 33, kSI = 580, kGS = 9264;
+constexpr uint32_t kOutJ = 16, kOutK = 32;
+static_assert(15 * kSI + (int)kOutJ * kSJ + (int)kOutK < kGS, "tile does not fit the layout");
+static_assert(kSI % 32 == 4 && kGS % 32 == 16 && kSJ % 32 == 1, "bank layout");
+// largest fixed-point scale: products stay below 2^22 so the FMA trick of
+// deposit4 converts them to integers exactly
+constexpr int kMaxFixBits = 23;
 // FP64 shared layout: dense [16][16][32]
 constexpr int kT3 = 16 * 16 * 32;
 // per-tile block counts: 4^3-cell blocks over the tile plus a 4-cell margin
@@ -431,7 +436,7 @@ struct __align__(16) StageRec {
     float4 w[3];      // per axis: PCS weights (k weights pre-scaled by 2^s)
 };
 
-__device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
+__device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, uint32_t outv) {
     uint32_t r = 0;
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
@@ -439,7 +444,7 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te) {
         cs += cs < 0 ? Ng : 0;
         cs -= cs >= Ng ? Ng : 0;
         const int l = cs - t0;
-        r |= (uint32_t)((unsigned)l < (unsigned)te ? l : 255) << (8 * s);
+        r |= ((unsigned)l < (unsigned)te ? (uint32_t)l : outv) << (8 * s);
     }
     return r;
 }
@@ -458,27 +463,26 @@ __device__ __forceinline__ void deposit4(uint32_t *acc, const StageRec *mystage,
     if (li == 255u) return;
     const float4 wxv = st.w[0], wy = st.w[1], wz = st.w[2];
     const float wa = a == 0 ? wxv.x : (a == 1 ? wxv.y : (a == 2 ? wxv.z : wxv.w));
-    // every update is issued: cells outside the tile go to this lane's trash
-    // word, so the 16 atomics run without branches
-    const uint32_t trash = kTrash + lane;
     const uint32_t plane = g * kGS + li * kSI;
-    uint32_t koff[4];
-#pragma unroll
-    for (int s4 = 0; s4 < 4; ++s4) koff[s4] = (loc.z >> (8 * s4)) & 255u;
+    const uint32_t k0 = loc.z & 255u, k1 = (loc.z >> 8) & 255u, k2 = (loc.z >> 16) & 255u, k3 = loc.z >> 24;
     const float wyv[4] = {wy.x, wy.y, wy.z, wy.w};
-    const float wzv[4] = {wz.x, wz.y, wz.z, wz.w};
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const uint32_t lj = (loc.y >> (8 * b)) & 255u;
-        const uint32_t row = plane + lj * kSJ;
+        uint32_t *row = acc + plane + ((loc.y >> (8 * b)) & 255u) * kSJ;
         const float w = wa * wyv[b];
-#pragma unroll
-        for (int s4 = 0; s4 < 4; ++s4) {
-            const uint32_t idx = (lj == 255u || koff[s4] == 255u) ? trash : row + koff[s4];
-            if (FIXED)
-                atomicAdd(acc + idx, __float2uint_rn(w * wzv[s4]));
-            else
-                atomicAdd(reinterpret_cast<float *>(acc) + idx, w * wzv[s4]);
+        if (FIXED) {
+            // round(w * wz) as an integer: FMA onto 1.5 * 2^23 (products < 2^22)
+            const float M = 12582912.0f;
+            atomicAdd(row + k0, __float_as_uint(fmaf(w, wz.x, M)) - 0x4B400000u);
+            atomicAdd(row + k1, __float_as_uint(fmaf(w, wz.y, M)) - 0x4B400000u);
+            atomicAdd(row + k2, __float_as_uint(fmaf(w, wz.z, M)) - 0x4B400000u);
+            atomicAdd(row + k3, __float_as_uint(fmaf(w, wz.w, M)) - 0x4B400000u);
+        } else {
+            float *rowf = reinterpret_cast<float *>(row);
+            atomicAdd(rowf + k0, w * wz.x);
+            atomicAdd(rowf + k1, w * wz.y);
+            atomicAdd(rowf + k2, w * wz.z);
+            atomicAdd(rowf + k3, w * wz.w);
         }
     }
 }
@@ -487,8 +491,8 @@ __global__ void __launch_bounds__(kPaintThreads, 2)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS] + trash[32]
-    StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS + 32);  // [warps][16][grids]
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS]
+    StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS);  // [warps][16][grids]
     uint32_t *blk = reinterpret_cast<uint32_t *>(stage + (kPaintThreads / 32) * kStageParts * kMaxPaintGrids);  // [kBlkN]
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
@@ -579,9 +583,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         if (tid == 0) {
             uint32_t m = 0;
             for (int w = 0; w < nwarp; ++w) m = max(m, scan_ws[w]);
-            int fb = 31;
+            int fb = kMaxFixBits;
             if (m > 0) fb = (int)floor(log2(4294967295.0 / ((double)m * kMaxCellWeight)));
-            fixbits_s = fb > 31 ? 31 : fb;
+            fixbits_s = fb > kMaxFixBits ? kMaxFixBits : fb;
         }
     }
     __syncthreads();
@@ -606,9 +610,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 cell_g((int)(rw[a] >> fb), rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
                 float w[4];
                 pcs_weights((float)dgq * inv, w);
+                const uint32_t outv = a == 0 ? 255u : (a == 1 ? kOutJ : kOutK);
                 uint32_t loc;
                 if (cyc[a]) {
-                    loc = pack_local(bg, Ng, ts.t0[a], ts.te[a]);
+                    loc = pack_local(bg, Ng, ts.t0[a], ts.te[a], outv);
                 } else {
                     // linear local index of the first stencil cell (periodic
                     // images folded to the nearest copy of the tile)
@@ -618,7 +623,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                     loc = 0;
 #pragma unroll
                     for (int s4 = 0; s4 < 4; ++s4)
-                        loc |= (uint32_t)((unsigned)(l + s4) < (unsigned)ts.te[a] ? l + s4 : 255) << (8 * s4);
+                        loc |= ((unsigned)(l + s4) < (unsigned)ts.te[a] ? (uint32_t)(l + s4) : outv) << (8 * s4);
                 }
                 st.loc[a] = loc;
                 const float sc = a == 2 ? fscale : 1.f;
@@ -883,7 +888,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
-        const size_t smem = sizeof(uint32_t) * (kMaxPaintGrids * kGS + 32) +
+        const size_t smem = sizeof(uint32_t) * kMaxPaintGrids * kGS +
                             sizeof(StageRec) * (kPaintThreads / 32) * kStageParts * kMaxPaintGrids +
                             sizeof(uint32_t) * kBlkN;
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
