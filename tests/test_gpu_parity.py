@@ -47,8 +47,11 @@ def grid_close(got, want, rel):
 
 # ---------------------------------------------------------------------------
 # src/tests/octet.c:8-62 through the C ABI
-@pytest.mark.parametrize("prec,eps", [("f64", 1e-15), ("f32", 1e-6)])
+@pytest.mark.parametrize("prec,eps", [("f64", 1e-15), ("f32", 1e-5)])
 def test_octet_known_answer(fg, prec, eps):
+    """The reference's eps = 1e-15 holds for FP64 grids.  FP32 grids paint in
+    fixed point with 2^-23 of a particle's weight per stencil cell and store
+    FP32, hence 1e-5 at this test's normalisation (x8)."""
     g = fg.Grid(2, 2.0, precision=prec)
     cat = fg.Catalog([-8.0], [-8.0], [-8.0], 8.0)
     off = g.p2g(cat, [7.0, 7.0, 7.0])
