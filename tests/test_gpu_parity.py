@@ -143,13 +143,18 @@ def test_small_cases_match_reference(fg, oracle_lib, small, prec, Ng):
             np.testing.assert_allclose(losh, losh_o, rtol=0, atol=0)
             np.testing.assert_allclose(got[:, 0], K, rtol=1e-6, equal_nan=True)
             den = np.abs(P[:, :1]) + Pshot
-            tol = 1e-6 if prec == "f64" else 1e-4
             ok = np.isfinite(P)
             assert np.all(np.isfinite(got[:, 2:]) == ok)
-            assert np.all(np.abs(got[:, 2:] - P)[ok] <= (tol * np.broadcast_to(den, P.shape))[ok] + 1e-300)
             Km, Nm, Pm, st2, _ = o.pmu(los, dK, 3)
             np.testing.assert_array_equal(gotm[:, 1::3], Nm)
-            assert np.all(np.abs(gotm[:, 2::3] - Pm) <= tol * (np.abs(Pm) + Pshot))
+            # FP64: every bin to 1e-6.  FP32: 1e-4 for k < 0.8 k_Nyq (the
+            # stated parity range), 1e-3 everywhere (the window deconvolution
+            # amplifies FP32 rounding ~200x in the corner of the cube)
+            sel = np.broadcast_to((K < 0.8 * np.pi * Ng / L)[:, None], P.shape)
+            for tol, mask in ([(1e-6, ok)] if prec == "f64" else [(1e-4, ok & sel), (1e-3, ok)]):
+                assert np.all(np.abs(got[:, 2:] - P)[mask] <= (tol * np.broadcast_to(den, P.shape))[mask] + 1e-300)
+                m2 = mask[:, :1].repeat(3, 1)
+                assert np.all((np.abs(gotm[:, 2::3] - Pm) <= tol * (np.abs(Pm) + Pshot))[m2])
 
 
 # ---------------------------------------------------------------------------
