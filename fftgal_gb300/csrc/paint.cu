@@ -449,30 +449,27 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, ui
     return r;
 }
 
-// deposit 4 staged particles: lane = (particle slot, grid, i row); every lane
-// adds its i row's 16 (j, k) cells, predicated on the packed validity bytes
+// deposit staged particles one at a time: lane = (grid, i row, j row), every
+// lane adds its row's 4 k cells.  By the bank layout the 32 rows of one
+// particle start in 32 distinct banks, so each of the 4 atomics is a single
+// shared-memory wavefront (the limiting resource of this kernel).  Cells
+// outside the tile land in the padding row / column.
 template <bool FIXED>
-__device__ __forceinline__ void deposit4(uint32_t *acc, const StageRec *mystage, int p0, int np, int ngr,
-                                         int lane) {
-    const int p = p0 + (lane >> 3);
-    const int g = (lane >> 2) & 1, a = lane & 3;
-    if (p >= np || g >= ngr) return;
-    const StageRec &st = mystage[p * kMaxPaintGrids + g];
-    const uint4 loc = *reinterpret_cast<const uint4 *>(st.loc);
-    const uint32_t li = (loc.x >> (8 * a)) & 255u;
-    if (li == 255u) return;
-    const float4 wxv = st.w[0], wy = st.w[1], wz = st.w[2];
-    const float wa = a == 0 ? wxv.x : (a == 1 ? wxv.y : (a == 2 ? wxv.z : wxv.w));
-    const uint32_t plane = g * kGS + li * kSI;
-    const uint32_t k0 = loc.z & 255u, k1 = (loc.z >> 8) & 255u, k2 = (loc.z >> 16) & 255u, k3 = loc.z >> 24;
-    const float wyv[4] = {wy.x, wy.y, wy.z, wy.w};
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        uint32_t *row = acc + plane + ((loc.y >> (8 * b)) & 255u) * kSJ;
-        const float w = wa * wyv[b];
+__device__ __forceinline__ void deposit_all(uint32_t *acc, const StageRec *mystage, int np, int ngr, int lane) {
+    const int g = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
+    if (g >= ngr) return;
+    const float M = 12582912.0f;  // 1.5 * 2^23: FMA onto it rounds w to an integer
+    for (int p = 0; p < np; ++p) {
+        const StageRec &st = mystage[p * kMaxPaintGrids + g];
+        const uint4 loc = *reinterpret_cast<const uint4 *>(st.loc);
+        const uint32_t li = (loc.x >> (8 * a)) & 255u;
+        if (li == 255u) continue;
+        const uint32_t lj = (loc.y >> (8 * b)) & 255u;
+        uint32_t *row = acc + g * kGS + li * kSI + lj * kSJ;
+        const float w = reinterpret_cast<const float *>(&st.w[0])[a] * reinterpret_cast<const float *>(&st.w[1])[b];
+        const float4 wz = st.w[2];
+        const uint32_t k0 = loc.z & 255u, k1 = (loc.z >> 8) & 255u, k2 = (loc.z >> 16) & 255u, k3 = loc.z >> 24;
         if (FIXED) {
-            // round(w * wz) as an integer: FMA onto 1.5 * 2^23 (products < 2^22)
-            const float M = 12582912.0f;
             atomicAdd(row + k0, __float_as_uint(fmaf(w, wz.x, M)) - 0x4B400000u);
             atomicAdd(row + k1, __float_as_uint(fmaf(w, wz.y, M)) - 0x4B400000u);
             atomicAdd(row + k2, __float_as_uint(fmaf(w, wz.z, M)) - 0x4B400000u);
@@ -633,9 +630,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         __syncwarp();
         const int np = min((uint32_t)kStageParts, total - base);
         if (fixed)
-            for (int p0 = 0; p0 < np; p0 += 4) deposit4<true>(acc, mystage, p0, np, ngr, lane);
+            deposit_all<true>(acc, mystage, np, ngr, lane);
         else
-            for (int p0 = 0; p0 < np; p0 += 4) deposit4<false>(acc, mystage, p0, np, ngr, lane);
+            deposit_all<false>(acc, mystage, np, ngr, lane);
         __syncwarp();
     }
     __syncthreads();
