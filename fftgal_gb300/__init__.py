@@ -97,6 +97,8 @@ SIGNATURES = {
     "fftgal_g2p_sum": (C.c_int, [_P_F, _P_G, _dp]),
     "fftgal_device_bytes": (C.c_long, [_P_F]),
     "fftgal_launch_count": (C.c_long, []),
+    "fftgal_power_bins_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_long, _dp,
+                                            C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp, C.c_void_p]),
 }
 
 NSTAGES = 11
@@ -338,6 +340,25 @@ class Grid:
                                       K.ctypes.data_as(_dp), N.ctypes.data_as(_lp), P.ctypes.data_as(_dp),
                                       Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))
         return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm)
+
+
+def power_bins_noalloc(fk: int, Ng: int, L: float, V: float, Np: int, los, dK: float, Nmu: int = 3,
+                       stream: int | None = None) -> dict:
+    """Multipoles and wedges of the deconvolved FP32 k-space grid at device
+    pointer ``fk`` without any GPU allocation (fftgal_power_bins_noalloc)."""
+    NK = lib().fftgal_nk(int(Ng), float(L), float(dK))
+    K = np.zeros(NK)
+    N = np.zeros(NK, dtype=np.int64)
+    P = np.zeros((NK, 4))
+    Km = np.zeros((NK, Nmu))
+    Nm = np.zeros((NK, Nmu), dtype=np.int64)
+    Pm = np.zeros((NK, Nmu))
+    l = _f64(los)
+    _check(lib().fftgal_power_bins_noalloc(int(fk), int(Ng), float(L), float(V), int(Np), l.ctypes.data_as(_dp),
+                                           float(dK), int(Nmu), K.ctypes.data_as(_dp), N.ctypes.data_as(_lp),
+                                           P.ctypes.data_as(_dp), Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp),
+                                           Pm.ctypes.data_as(_dp), stream))
+    return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm)
 
 
 def nk(Ng: int, L: float, dK: float) -> int:

@@ -101,6 +101,35 @@ int fftgal_g2p_sum(fft_t *grid, const gal_t *pos, double *out);
 /* bytes of GPU memory held by the grid (grids, scratch, tables) */
 long fftgal_device_bytes(fft_t *grid);
 
+/* Multipoles and wedges of a deconvolved FP32 k-space grid that is already in
+ * GPU memory, without allocating GPU memory.  No counterpart in the
+ * reference: it serves callers that cannot allocate -- a host framework that
+ * owns all device memory through its own pool, code that must not call
+ * cudaMalloc/cudaFree because they synchronise the device, or a process whose
+ * device memory is committed in advance.  It calls no cudaMalloc, cudaFree or
+ * allocating library routine.
+ *   fk         Ng*Ng*(Ng/2+1) complex FP32 values in the layout of the
+ *              canonical grid (rows of Ng+2 floats), e.g. fftgal_device_grid()
+ *              after fftgal_power_f32 or fft_p2k on an FP32 grid
+ *   V, Np      P = |fk|^2 / V - V / Np (src/power.c:55)
+ *   los, dK, Nmu, outputs: as fftgal_power_f32 (outputs on the host)
+ *   stream     cudaStream_t to run on (NULL: the legacy default stream); the
+ *              call returns after the results are on the host
+ * Scratch is one fixed array of about 1.8 MB in the library's device memory,
+ * shared by all calls: it holds the k-bin limits, per-bin sums and counts of
+ * the last call and is cleared at the start of each.  Calls whose GPU work
+ * overlaps (from several host threads, or on several streams) race on it.
+ * Limits: NK <= 2048 k bins, 1 <= Nmu <= 16, Ng <= 4096, and the per-block
+ * accumulators (about 12 * NK * (2*Nmu + 6) bytes) within 220 KB of shared
+ * memory; larger requests return FFTGAL_ERR_RANGE / FFTGAL_ERR_UNSUPPORTED.
+ * The first call on each device looks up the scratch's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. */
+int fftgal_power_bins_noalloc(const float *fk, int Ng, double L, double V, long Np,
+                              const double los[3], double dK, int Nmu, double *K,
+                              long *N, double *Pl, double *Kmu, long *Nmu_count,
+                              double *Pmu, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
