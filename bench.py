@@ -119,9 +119,10 @@ class ClockSampler:
 # CPU oracle baseline (bounded sample, extrapolated to the full workload)
 def cpu_sample(seed: int = 1, Ng: int = 256, scale: int = 64):
     """Time the FP64 oracle (p2k + P + Pl + Pmu, src/fft.c:257-276,
-    src/power.c:12-178 restated in C) on Ng=256 with Np/64 particles -- the
-    full workload's particle density -- and extrapolate to Ng=1024, 1e8:
-    particle, grid and binning work x64, FFT work x64 x 30/24 (N log N).
+    src/power.c:12-178 restated in C) on an Ng grid with Np/scale particles
+    (scale = (1024/Ng)^3 keeps the full workload's particle density) and
+    extrapolate to Ng=1024, 1e8: particle, grid and binning work x scale, FFT
+    work x scale x log(1024^3)/log(Ng^3) (N log N).
     Returns (seconds per full catalog, sample seconds)."""
     import numpy as np
     import oracle
@@ -144,13 +145,13 @@ def cpu_sample(seed: int = 1, Ng: int = 256, scale: int = 64):
     g.x2k(0)
     t_fft = time.perf_counter() - t1
     lin = max(t_all - 2 * t_fft, 0.0)
-    full = lin * scale + 2 * t_fft * scale * (30.0 / 24.0)
+    full = lin * scale + 2 * t_fft * scale * (math.log2(NG ** 3) / math.log2(Ng ** 3))
     return full, t_all + t_fft
 
 
 def _cpu_worker(args):
     seed, Ng = args
-    return cpu_sample(seed, Ng)
+    return cpu_sample(seed, Ng, (NG // Ng) ** 3)
 
 
 def run_reference(args):
@@ -218,8 +219,8 @@ def algorithmic_bytes(Ng: int, Np: int):
         "fft_k": 2 * (R4 + G4),                # both grids, read real rows, write half spectra
         "fft_j": 2 * 2 * G4,
         "fft_i": 2 * 2 * G4,
-        "finish": 3 * G4,                      # read both grids, write one
-        "bin": G4,
+        "finish": 0,                           # fused into finish_bin
+        "finish_bin": 3 * G4,                  # read both grids, write one, bin its power
     }
 
 
@@ -335,10 +336,10 @@ def run_ours(args):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            full, wall = cpu_sample()
+            full, wall = cpu_sample(1, 512, 8)
             cpu = {"value": 1.0 / full, "unit": "catalogs/s", "cores": 1, "kind": "port",
-                   "sample": f"FP64 oracle (src/fft.c + src/power.c restated), Ng=256, Np=1.5625e6 uniform, "
-                             f"{wall:.1f}s, extrapolated to Ng=1024/1e8 (x64, FFT x64x30/24)"}
+                   "sample": f"FP64 oracle (src/fft.c + src/power.c restated), Ng=512, Np=1.25e7 uniform, "
+                             f"{wall:.1f}s, extrapolated to Ng=1024/1e8 (x8, FFT x8x30/27)"}
         out = {
             "metric": METRIC, "value": value, "unit": "catalogs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

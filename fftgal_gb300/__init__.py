@@ -103,7 +103,7 @@ SIGNATURES = {
 
 NSTAGES = 11
 STAGES = ["upload", "paint_key", "paint_scan", "paint_scatter", "paint_tile", "fft_k", "fft_j",
-          "fft_i", "finish", "bin", "total"]
+          "fft_i", "finish", "finish_bin", "total"]
 
 _lib = None
 

@@ -91,7 +91,8 @@ struct Grid {
     size_t pos_cap = 0;     // bytes
     void *d_stage = nullptr;  // host-double staging for uploads
     size_t stage_cap = 0;
-    double *d_tab = nullptr;  // [3][Ng] complex phase table, [Ng] winv, [3][Ng] offset-1/2 phase
+    double *d_tab = nullptr;  // [3][Ng] complex phase table, [Ng] winv, [3][Ng] offset-1/2 phase,
+                              // then FP32 copies: [3][Ng] offset-1/2 phase, [Ng] winv
     BinGeometry geo[kGeoCache];
     int geo_next = 0;
     unsigned long version = 1;  // bumped whenever the grid changes
@@ -216,7 +217,7 @@ static int ensure_aux(Grid *g) {
 static int ensure_tables(Grid *g) {
     if (g->d_tab) return OK;
     const size_t Ng = g->Ng;
-    FG_CUDA(cudaMalloc(&g->d_tab, sizeof(double) * (13 * Ng)));
+    FG_CUDA(cudaMalloc(&g->d_tab, sizeof(double) * (17 * Ng)));
     std::vector<double> w(Ng);
     build_winv_table(w.data(), g->Ng);
     FG_CUDA(cudaMemcpy(g->d_tab + 6 * Ng, w.data(), sizeof(double) * Ng, cudaMemcpyHostToDevice));
@@ -225,11 +226,18 @@ static int ensure_tables(Grid *g) {
     const double half[3] = {remainder(0.5, g->Ng), remainder(0.5, g->Ng), remainder(0.5, g->Ng)};
     build_phase_table(ph.data(), g->Ng, half, 1);
     FG_CUDA(cudaMemcpy(g->d_tab + 7 * Ng, ph.data(), sizeof(double) * 6 * Ng, cudaMemcpyHostToDevice));
+    // FP32 copies of both for the fused finish + binning pass
+    std::vector<float> t32(7 * Ng);
+    for (size_t e = 0; e < 6 * Ng; ++e) t32[e] = (float)ph[e];
+    for (size_t e = 0; e < Ng; ++e) t32[6 * Ng + e] = (float)w[e];
+    FG_CUDA(cudaMemcpy(g->d_tab + 13 * Ng, t32.data(), sizeof(float) * 7 * Ng, cudaMemcpyHostToDevice));
     return OK;
 }
 
 static const double *winv_tab(const Grid *g) { return g->d_tab + 6 * (size_t)g->Ng; }
 static const double *dual_tab(const Grid *g) { return g->d_tab + 7 * (size_t)g->Ng; }
+static const float *dual_tab32(const Grid *g) { return reinterpret_cast<const float *>(g->d_tab + 13 * (size_t)g->Ng); }
+static const float *winv_tab32(const Grid *g) { return dual_tab32(g) + 6 * (size_t)g->Ng; }
 
 static int phase(Grid *g, void *dst, const double offset[3], int onoff) {
     FG_TRY(ensure_tables(g));
@@ -655,7 +663,7 @@ namespace fg {
 // caches the wedge sums for a following Pmu on the same grid version
 static int bin_pass(fft_t *grid, const double los_hat[3], double dK, int Nmu, BinGeometry **geo_out,
                     std::vector<double> &Psum, std::vector<double> &Pw, int mode, double Vinv, double Pshot,
-                    cudaEvent_t *ev_end = nullptr) {
+                    cudaEvent_t *ev_end = nullptr, const BinFinish *fin = nullptr) {
     Grid *g = G(grid);
     BinSpec s;
     FG_TRY(bin_spec_init(&s, grid->Ng, grid->L, dK, los_hat, Nmu));
@@ -665,7 +673,7 @@ static int bin_pass(fft_t *grid, const double los_hat[3], double dK, int Nmu, Bi
         return set_error(ERR_RANGE, "a mode falls beyond the last of NK=%d k bins (dK too small for Ng)", s.NK);
     Psum.assign((size_t)s.NK * 4, 0.0);
     Pw.assign((size_t)s.NK * (Nmu + 1), 0.0);
-    FG_TRY(bin_power(geo, g->d_f, g->prec, mode, Vinv, Pshot, Psum.data(), Pw.data(), g->stream, ev_end));
+    FG_TRY(bin_power(geo, g->d_f, g->prec, mode, Vinv, Pshot, Psum.data(), Pw.data(), g->stream, ev_end, fin));
     *geo_out = geo;
     return OK;
 }
@@ -960,8 +968,6 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
     FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
-    FG_TRY(interlace_finish(g->d_f, g->d_aux, Ng, 4, H3, dual_tab(g), winv_tab(g), st));
-    if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
     for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
     ++g->version;
     double los[3] = {los_in[0], los_in[1], los_in[2]};
@@ -970,7 +976,16 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     std::vector<double> Psum, Pw;
     const double Vinv = 1 / V;
     const double Pshot = V / Np;
-    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, 1, Vinv, Pshot, tm ? &ev[10] : nullptr));
+    // interlacing finish (offset phase, average, deconvolution) fused into the
+    // binning pass; the finish stage is timed as part of the binning stage
+    BinFinish fin;
+    fin.A = g->d_f;
+    fin.B = g->d_aux;
+    fin.ph32 = dual_tab32(g);
+    fin.w32 = winv_tab32(g);
+    fin.scale = 0.5 * H3;
+    if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
+    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, 2, Vinv, Pshot, tm ? &ev[10] : nullptr, &fin));
     if (tm) {
         FG_CUDA(cudaEventSynchronize(ev[kStages]));
         float ms;

@@ -284,58 +284,110 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
         if (acc64[e] != 0) atomicAdd(&gacc[e], acc64[e]);
 }
 
-// FP32 grids: one thread per contiguous run of kSegModes modes of a k row.
-// Along k the k bin is non-decreasing, so the thread keeps running sums in
-// registers and flushes them to shared memory only when the bin (or, for the
-// wedge sums, the (bin, wedge) pair) changes.  Shared accumulators are laid
-// out [quantity][bin] so neighbouring bins fall in neighbouring banks.
-constexpr int kSegModes = 16;
+// FP32 grids.  The half spectrum is cut into blocks of 16 (i) x 16 (j) x 32
+// (k) modes.  Each warp of a CTA stages one 16 x 32 slab of the block (16
+// rows of 32 consecutive k, from coalesced loads) as FP32 powers in shared
+// memory, then walks the slab in runs of 16 modes along the grid axis whose
+// |n_a| is smallest at the block's centre: along that axis |n| changes
+// slowest, so a run crosses the fewest k-bin edges (about 0.3 per mode,
+// against 0.55 along a fixed axis).  A thread keeps the run's sums in
+// registers and adds them to the CTA's FP32 shared accumulators when the bin
+// (or the wedge) changes; every kFoldBlocks blocks the CTA adds its FP32
+// sums to the FP64 global accumulators.
+//   MODE 0: the grid holds P in F_Re (after P()).
+//   MODE 1: the grid holds delta; P = |delta|^2 Vinv - Pshot.
+//   MODE 2: as 1, with the interlacing finish of the grid fused in: A <-
+//           (A + B * phase) * W^-1 * scale is written back and binned.
+constexpr int kSlabI = 16, kSlabJ = 16, kSlabK = 32, kSlabRow = 33;
+constexpr int kSlabThreads = 512;  // one warp per slab of a block
+constexpr int kFoldBlocks = 8;
+
+struct SlabFinish {
+    float2 *A = nullptr;
+    const float2 *B = nullptr;
+    const float2 *ph = nullptr;  // [3][Ng] phase of the interlacing grid (FP32)
+    const float *w = nullptr;    // [Ng] PCS window inverse (FP32)
+    float scale = 0.f;           // H^3 / 2
+};
 
 template <int MODE>
-__global__ void __launch_bounds__(kBinThreads)
-bin_power_seg_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Pshot,
-                     const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, int Ng_pad) {
+__global__ void __launch_bounds__(kSlabThreads, 3)
+bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, float Vinv, float Pshot,
+                      const uint32_t *__restrict__ thr_g, double *__restrict__ gacc) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int NK = d.NK, W = d.W, NQ = 4 + W;
-    double *acc64 = reinterpret_cast<double *>(smem_raw);               // [NQ][NK]
-    float *acc32 = reinterpret_cast<float *>(acc64 + (size_t)NK * NQ);  // [NQ][NK]
-    uint32_t *thr = reinterpret_cast<uint32_t *>(acc32 + (size_t)NK * NQ);
-    const int tid = threadIdx.x;
-    for (int e = tid; e < NK * NQ; e += blockDim.x) {
-        acc64[e] = 0;
-        acc32[e] = 0.f;
-    }
+    float *acc32 = reinterpret_cast<float *>(smem_raw);                        // [NQ][NK]
+    uint32_t *thr = reinterpret_cast<uint32_t *>(acc32 + (size_t)NK * NQ);     // [NK + 2]
+    float *slabs = reinterpret_cast<float *>(thr + ((NK + 2 + 3) & ~3));        // [16][16][kSlabRow]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float *slab = slabs + warp * kSlabJ * kSlabRow;
+    for (int e = tid; e < NK * NQ; e += blockDim.x) acc32[e] = 0.f;
     for (int e = tid; e < NK + 2; e += blockDim.x) thr[e] = thr_g[e];
     __syncthreads();
-
     const int Ng = d.Ng, nh = d.nh;
-    const int nrows = Ng * Ng;
-    const int nsegr = (nh + kSegModes - 1) / kSegModes;
-    const int nchunks = (nrows + kChunkRows - 1) / kChunkRows;
-    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-        const int r0 = ch * kChunkRows;
-        const int nitems = (min(nrows, r0 + kChunkRows) - r0) * nsegr;
-        for (int it = tid; it < nitems; it += blockDim.x) {
-            const int row = r0 + it / nsegr, seg = it % nsegr;
-            const int i = row / Ng, j = row - i * Ng;
-            const int ki = kval(i, Ng), kj = kval(j, Ng);
-            const int n2ij = ki * ki + kj * kj;
-            const float *frow = f + (long)row * Ng_pad;
+    const int nbi = (Ng + kSlabI - 1) / kSlabI, nbj = (Ng + kSlabJ - 1) / kSlabJ, nbk = (nh + kSlabK - 1) / kSlabK;
+    const int nblk = nbi * nbj * nbk;
+    int since_fold = 0;
+    for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        const int bk = blk % nbk, bj = (blk / nbk) % nbj, bi = blk / (nbk * nbj);
+        const int i0 = bi * kSlabI, j0 = bj * kSlabJ, k0 = bk * kSlabK;
+        const int ci = abs(kval(min(i0 + kSlabI / 2, Ng - 1), Ng));
+        const int cj = abs(kval(min(j0 + kSlabJ / 2, Ng - 1), Ng));
+        const int ck = min(k0 + kSlabK / 2, nh - 1);
+        const int axis = (ck <= ci && ck <= cj) ? 2 : (cj <= ci ? 1 : 0);  // run axis
+        // the warp's slab: for runs along i it fixes j and its rows are i,
+        // otherwise it fixes i and its rows are j
+        const bool rows_i = axis == 0;
+        const int fixed = (rows_i ? j0 : i0) + warp;
+        const int r0 = rows_i ? i0 : j0;
+        const int k = k0 + lane;
+        if (fixed < Ng) {
+            float2 pfk = make_float2(0.f, 0.f);
+            float wfk = 0.f;
+            if (MODE == 2 && k < nh) {
+                pfk = cmul(fin.ph[(rows_i ? Ng : 0) + fixed], fin.ph[2 * Ng + k]);
+                wfk = fin.w[fixed] * fin.w[k] * fin.scale;
+            }
+#pragma unroll 4
+            for (int r = 0; r < kSlabJ; ++r) {
+                const int rr = r0 + r;
+                float pv = 0.f;
+                if (rr < Ng && k < nh) {
+                    const long e = (rows_i ? ((long)rr * Ng + fixed) : ((long)fixed * Ng + rr)) * nh + k;
+                    if (MODE == 2) {
+                        const float2 p = cmul(pfk, fin.ph[(rows_i ? 0 : Ng) + rr]);
+                        const float wk = wfk * fin.w[rr];
+                        const float2 bv = fin.B[e], av = fin.A[e];
+                        const float2 dv = cmul(bv, p);
+                        const float2 v = make_float2((dv.x + av.x) * wk, (dv.y + av.y) * wk);
+                        fin.A[e] = v;
+                        pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+                    } else if (MODE == 1) {
+                        const float2 v = f[e];
+                        pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+                    } else {
+                        pv = f[e].x;
+                    }
+                }
+                slab[r * kSlabRow + lane] = pv;
+            }
+        }
+        __syncwarp();
+        if (fixed < Ng) {
+            // runs along k: lane = (row, half of the 32 k); else lane = k
+            int r = axis == 2 ? (lane & 15) : 0, c = axis == 2 ? 16 * (lane >> 4) : lane;
+            const int dr = axis == 2 ? 0 : 1, dc = axis == 2 ? 1 : 0;
             int cb = -1, cm = -1;
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, sw = 0.f;
-            const int k1 = min(nh, (seg + 1) * kSegModes);
-            for (int k = seg * kSegModes; k < k1; ++k) {
-                if ((row | k) == 0) continue;  // the k = 0 mode (src/power.c:52-54)
-                const int kk = kval(k, Ng);
-                const uint32_t n2 = (uint32_t)(n2ij + kk * kk);
-                float p;
-                if constexpr (MODE == 0) {
-                    p = frow[2 * k];
-                } else {
-                    const float2 v = reinterpret_cast<const float2 *>(frow)[k];
-                    p = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
-                }
-                const float pc = (k != 0 && 2 * k != Ng) ? 2.f * p : p;  // count 1 + (2k % Ng > 0)
+            for (int t = 0; t < 16; ++t, r += dr, c += dc) {
+                const int rr = r0 + r, kc = k0 + c;
+                if (rr >= Ng || kc >= nh) continue;
+                const int i = rows_i ? rr : fixed, j = rows_i ? fixed : rr;
+                if ((i | j | kc) == 0) continue;  // the k = 0 mode (src/power.c:52-54)
+                const int ki = kval(i, Ng), kj = kval(j, Ng), kk = kval(kc, Ng);
+                const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
+                const float p = slab[r * kSlabRow + c];
+                const float pc = (kc != 0 && 2 * kc != Ng) ? 2.f * p : p;  // count 1 + (2k % Ng > 0)
                 const float n2f = (float)n2;
                 const float rk = rsqrtf(n2f);
                 int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
@@ -372,57 +424,96 @@ bin_power_seg_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Ps
                 atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
             }
         }
-        __syncthreads();
-        for (int e = tid; e < NK * NQ; e += blockDim.x) {
-            acc64[e] += (double)acc32[e];
-            acc32[e] = 0.f;
+        __syncwarp();
+        if (++since_fold == kFoldBlocks) {
+            since_fold = 0;
+            __syncthreads();
+            for (int e = tid; e < NK * NQ; e += blockDim.x) {
+                const float v = acc32[e];
+                if (v != 0.f) {
+                    const int q = e / NK, b = e - q * NK;
+                    atomicAdd(&gacc[(size_t)b * NQ + q], (double)v);
+                    acc32[e] = 0.f;
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
-    // back to the [bin][quantity] layout of the global accumulators
+    __syncthreads();
     for (int e = tid; e < NK * NQ; e += blockDim.x) {
-        const int q = e / NK, b = e - q * NK;
-        if (acc64[e] != 0) atomicAdd(&gacc[(size_t)b * NQ + q], acc64[e]);
+        const float v = acc32[e];
+        if (v != 0.f) {
+            const int q = e / NK, b = e - q * NK;
+            atomicAdd(&gacc[(size_t)b * NQ + q], (double)v);
+        }
     }
 }
 
+static size_t slab_smem(int NK, int NQ) {
+    return sizeof(float) * (size_t)NK * NQ + sizeof(uint32_t) * (size_t)((NK + 2 + 3) & ~3) +
+           sizeof(float) * (kSlabThreads / 32) * kSlabJ * kSlabRow;
+}
+
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
-              double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end) {
+              double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end, const BinFinish *fin) {
     if (!g->valid) return set_error(ERR_STATE, "bin geometry not built");
+    if (mode == 2 && (prec != 4 || !fin)) return set_error(ERR_ARG, "fused finish needs an FP32 grid");
     const BinSpec &s = g->spec;
     const BinDev d = make_dev(s);
     const int NK = s.NK, W = s.Nmu + 1, NQ = 4 + W;
-    size_t smem = (size_t)NK * NQ * 8 + (prec == 4 ? (size_t)NK * NQ * 4 : 0) + sizeof(uint32_t) * (NK + 2);
+    const size_t smem = prec == 4 ? slab_smem(NK, NQ) : (size_t)NK * NQ * 8 + sizeof(uint32_t) * (NK + 2);
     if (smem > 220 * 1024)
         return set_error(ERR_UNSUPPORTED, "binning: %d k bins x %d wedges exceed shared memory", NK, s.Nmu);
     FG_CUDA(cudaMemsetAsync(g->d_acc, 0, sizeof(double) * g->acc_len, st));
-    const int Ng_pad = 2 * (s.Ng / 2 + 1);
-    const long nchunks = ceil_div((long)s.Ng * s.Ng, kChunkRows);
-    int per_sm = (int)((220 * 1024) / smem);
-    per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
-    long nb = (long)num_sms() * per_sm;
-    if (nb > nchunks) nb = nchunks;
-#define FG_BIN_LAUNCH(T, M)                                                                            \
-    do {                                                                                               \
-        FG_CUDA(cudaFuncSetAttribute(bin_power_kernel<T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                     (int)smem));                                                      \
-        bin_power_kernel<T, M><<<(unsigned)nb, kBinThreads, smem, st>>>(                               \
-            d, (const T *)f, (T)Vinv, (T)Pshot, g->d_thr, g->d_acc, Ng_pad);                           \
-    } while (0)
     if (prec == 4) {
-        if (mode == 0) {
-            FG_CUDA(cudaFuncSetAttribute(bin_power_seg_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            bin_power_seg_kernel<0><<<(unsigned)nb, kBinThreads, smem, st>>>(d, (const float *)f, (float)Vinv,
-                                                                            (float)Pshot, g->d_thr, g->d_acc, Ng_pad);
-        } else {
-            FG_CUDA(cudaFuncSetAttribute(bin_power_seg_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            bin_power_seg_kernel<1><<<(unsigned)nb, kBinThreads, smem, st>>>(d, (const float *)f, (float)Vinv,
-                                                                            (float)Pshot, g->d_thr, g->d_acc, Ng_pad);
+        int per_sm = (int)((224 * 1024) / (smem + 1024));
+        per_sm = per_sm < 1 ? 1 : (per_sm > 3 ? 3 : per_sm);
+        const long nblk = ceil_div(s.Ng, kSlabI) * ceil_div(s.Ng, kSlabJ) * ceil_div(s.Ng / 2 + 1, kSlabK);
+        long nb = (long)num_sms() * per_sm;
+        if (nb > nblk) nb = nblk;
+        SlabFinish sf;
+        if (fin) {
+            sf.A = static_cast<float2 *>(fin->A);
+            sf.B = static_cast<const float2 *>(fin->B);
+            sf.ph = static_cast<const float2 *>(fin->ph32);
+            sf.w = static_cast<const float *>(fin->w32);
+            sf.scale = (float)fin->scale;
         }
+        const float2 *fv = static_cast<const float2 *>(mode == 2 ? fin->A : f);
+#define FG_SLAB_LAUNCH(M)                                                                                   \
+    do {                                                                                                    \
+        FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                     (int)smem));                                                           \
+        bin_power_slab_kernel<M><<<(unsigned)nb, kSlabThreads, smem, st>>>(d, fv, sf, (float)Vinv, (float)Pshot, \
+                                                                         g->d_thr, g->d_acc);               \
+    } while (0)
+        if (mode == 0)
+            FG_SLAB_LAUNCH(0);
+        else if (mode == 1)
+            FG_SLAB_LAUNCH(1);
+        else
+            FG_SLAB_LAUNCH(2);
+#undef FG_SLAB_LAUNCH
     } else {
-        if (mode == 0) FG_BIN_LAUNCH(double, 0); else FG_BIN_LAUNCH(double, 1);
-    }
+        const int Ng_pad = 2 * (s.Ng / 2 + 1);
+        const long nchunks = ceil_div((long)s.Ng * s.Ng, kChunkRows);
+        int per_sm = (int)((220 * 1024) / smem);
+        per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
+        long nb = (long)num_sms() * per_sm;
+        if (nb > nchunks) nb = nchunks;
+#define FG_BIN_LAUNCH(M)                                                                                     \
+    do {                                                                                                     \
+        FG_CUDA(cudaFuncSetAttribute(bin_power_kernel<double, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                                            \
+        bin_power_kernel<double, M><<<(unsigned)nb, kBinThreads, smem, st>>>(                                \
+            d, (const double *)f, Vinv, Pshot, g->d_thr, g->d_acc, Ng_pad);                                  \
+    } while (0)
+        if (mode == 0)
+            FG_BIN_LAUNCH(0);
+        else
+            FG_BIN_LAUNCH(1);
 #undef FG_BIN_LAUNCH
+    }
     FG_LAUNCHED(1);
     if (ev_end) FG_CUDA(cudaEventRecord(*ev_end, st));
     std::vector<double> h(g->acc_len);

@@ -173,12 +173,23 @@ struct BinGeometry {               // data-independent part, cached
 int bin_spec_init(BinSpec *b, int Ng, double L, double dK, const double los_hat[3], int Nmu);
 int bin_geometry_build(BinGeometry *g, const BinSpec &spec, cudaStream_t st);
 void bin_geometry_free(BinGeometry *g);
+// interlacing finish fused into the FP32 binning pass (mode 2 of bin_power)
+struct BinFinish {
+    void *A = nullptr;           // canonical grid, finished in place
+    const void *B = nullptr;     // interlacing grid
+    const void *ph32 = nullptr;  // [3][Ng] float2 phase of the interlacing grid
+    const void *w32 = nullptr;   // [Ng] float PCS window inverse
+    double scale = 0;            // H^3 / 2
+};
 // power sums over the half spectrum.  mode 0: input holds P (F_Re = P, from P());
-// mode 1: input holds delta (complex), P = |delta|^2 * Vinv - Pshot computed on the fly.
+// mode 1: input holds delta (complex), P = |delta|^2 * Vinv - Pshot computed on the fly;
+// mode 2 (FP32): `fin` names both interlacing grids, A <- (A + B phase) W^-1 H^3/2
+// is written back and binned as in mode 1 (`f` unused).
 // Results (host): Psum[NK][4] (count-weighted, times Legendre), Pw[NK][Nmu+1].
 // `ev_end` (optional) is recorded right after the binning kernel
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
-              double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end = nullptr);
+              double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end = nullptr,
+              const BinFinish *fin = nullptr);
 
 // ---- misc -----------------------------------------------------------------------
 int num_sms();

@@ -85,8 +85,9 @@ int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z
 /* Per-stage device times (ms) of the last fftgal_power_f32 call, measured with
  * CUDA events on the grid's stream: [0] position upload, [1] paint key +
  * histogram, [2] histogram scan, [3] scatter, [4] tile paint, [5] FFT k pass,
- * [6] FFT j pass, [7] FFT i pass, [8] phase + average + deconvolution,
- * [9] binning, [10] total.  Enabled with fftgal_set_timing(grid, 1). */
+ * [6] FFT j pass, [7] FFT i pass, [8] nothing (the interlacing finish --
+ * offset phase, average, deconvolution -- runs inside [9]), [9] finish +
+ * binning, [10] total.  Enabled with fftgal_set_timing(grid, 1). */
 #define FFTGAL_NSTAGES 11
 int fftgal_set_timing(fft_t *grid, int on);
 int fftgal_stage_times(fft_t *grid, double out_ms[FFTGAL_NSTAGES]);
