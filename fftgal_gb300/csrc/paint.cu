@@ -18,15 +18,16 @@
 //               accumulates their weights in shared memory and writes every
 //               owned cell exactly once (no global atomics, no zeroing pass).
 //
-// FP32 grids (paint_coop_kernel): each lane prepares one particle (cell
-// indices and the 3 x 4 weights of both grids) in shared memory, then the warp
-// deposits the particles one at a time with lane = (grid, i row, j row), each
-// lane adding its 4 k cells.  The shared layout puts those 32 rows in 32
-// distinct banks.  Sums are 32-bit fixed point with a per-tile scale 2^-s: a
-// first pass counts particles per 4^3-cell block, and s is the largest value
-// for which no cell can exceed 2^32 (a particle adds at most (2/3)^3 of its
-// weight to a cell).  Integer sums are order independent, so the painted grid
-// is bit-reproducible run to run.
+// FP32 grids (paint_coop_kernel, persistent over tiles): each lane prepares
+// one particle (cell indices and the 3 x 4 weights of one grid) in shared
+// memory, then the warp deposits the particles one at a time with lane =
+// (grid, i row, j row), each lane adding its 4 k cells; the shared layout makes
+// every such step touch 32 distinct banks.  Sums are 32-bit fixed point with a
+// per-tile scale 2^-s, s the largest value for which no cell can exceed 2^32 (a
+// particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
+// total bounds every cell, and only where that bound costs precision does a
+// first pass count particles per 4^3-cell block.  Integer sums are order
+// independent, so the painted grid is bit-reproducible run to run.
 // FP64 grids (paint_tile_f64_kernel) reproduce the reference's FP64 weight
 // arithmetic op for op and accumulate in FP64, one thread per particle.
 #include "internal.h"
@@ -40,17 +41,24 @@ namespace fg {
 
 constexpr int kTileExt[3] = {16, 16, 32};    // i, j, k
 constexpr int kMaxPaintGrids = 2;
-constexpr double kMaxCellWeight = 8.0 / 27.0;  // largest PCS weight product
 constexpr int kMinFixBits = 8;                 // below this: FP32 accumulation
-// FP32 shared layout: cell (li, lj, lk) of grid g at g*kGS + li*kSI + lj*kSJ + lk;
-// kSJ = 1, kSI = 4, kGS = 16 (mod 32) gives the 32 rows (g, li+a, lj+b),
-// a, b < 4, of one stencil 32 distinct banks.  Row lj = 16 and column lk = 32
-// are padding that absorbs the updates of stencil cells outside the tile, so
-// the deposit needs no per-cell test.
-constexpr int kSJ = 33, kSI = 580, kGS = 9264;
-constexpr uint32_t kOutJ = 16, kOutK = 32;
-static_assert(15 * kSI + (int)kOutJ * kSJ + (int)kOutK < kGS, "tile does not fit the layout");
-static_assert(kSI % 32 == 4 && kGS % 32 == 16 && kSJ % 32 == 1, "bank layout");
+// FP32 shared layout: cell (li, lj, lk) of grid g at g*kGS + li*kSI + lj*kSJ +
+// kPadK + lk.  kSI = 8 and kSJ = 6 (mod 32) put the 16 rows (li+a, lj+b), a, b
+// < 4, of one stencil in 16 distinct banks of one parity, and the odd kGS gives
+// the other grid the other parity: with each lane of the second grid taking
+// its 4 k cells in the order s ^ ((b1 - b0) & 1) (its stencil is shifted by
+// b1 - b0 cells along k), every one of the 4 atomic steps of a particle touches
+// 32 distinct banks.  kPadK columns on either side of a row take the stencil
+// cells beyond the tile along k, so a particle's 4 k cells are always
+// contiguous; stencil rows outside the tile in i or j (local index kOut) are
+// skipped.
+constexpr int kPadK = 3;
+constexpr int kSJ = 38, kSI = 616, kGS = 9849;
+constexpr uint32_t kOut = 255u;
+static_assert(15 * kSI + 15 * kSJ + kSJ <= kGS, "tile does not fit the layout");
+static_assert(32 + 2 * kPadK <= kSJ, "row padding");
+static_assert(kSI % 32 == 8 && kSJ % 32 == 6 && kGS % 2 == 1, "bank layout");
+constexpr size_t kAccBytes = (sizeof(uint32_t) * 2 * kGS + 15) / 16 * 16;
 // largest fixed-point scale: products stay below 2^22 so the FMA trick of
 // deposit4 converts them to integers exactly
 constexpr int kMaxFixBits = 23;
@@ -360,54 +368,64 @@ struct TileSegs {
     uint32_t total;
 };
 
-__device__ void tile_segments(const PaintParams &pp, const uint32_t *__restrict__ off, uint32_t *seg_begin,
-                              uint32_t *seg_pref, uint32_t *scan_ws, TileSegs &ts) {
-    const int nt0 = pp.nt[0], nt1 = pp.nt[1], nt2 = pp.nt[2];
-    const int tt[3] = {(int)(blockIdx.x / (nt1 * nt2)), (int)((blockIdx.x / nt2) % nt1), (int)(blockIdx.x % nt2)};
-    (void)nt0;
-    int nopt[3], otile[3][5], ocls[3][5];
+__device__ void tile_geometry(const PaintParams &pp, unsigned tile, TileSegs &ts) {
+    const int nt1 = pp.nt[1], nt2 = pp.nt[2];
+    const int tt[3] = {(int)(tile / (nt1 * nt2)), (int)((tile / nt2) % nt1), (int)(tile % nt2)};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         ts.t0[a] = pp.start[a][tt[a]];
         ts.te[a] = pp.start[a][tt[a] + 1] - ts.t0[a];
-        const int nt = pp.nt[a];
-        int k = 0;
-        if (nt == 1) {
-            otile[a][k] = tt[a];
-            ocls[a][k++] = 0;
-        } else {
-            for (int c = 0; c < 3; ++c) {
-                otile[a][k] = tt[a];
-                ocls[a][k++] = c;
-            }
-            const int lo = (tt[a] + nt - 1) % nt, hi = (tt[a] + 1) % nt;
-            if (nt == 2) {
-                otile[a][k] = hi;
-                ocls[a][k++] = 1;
-                otile[a][k] = hi;
-                ocls[a][k++] = 2;
+    }
+}
+
+// thread q's segment of `tile` (q < the returned count): first sorted index b
+// and length cnt.  Issued a tile ahead so the loads overlap the write-out.
+__device__ int tile_segment(const PaintParams &pp, const uint32_t *__restrict__ off, unsigned tile, int q,
+                            uint32_t &b, uint32_t &cnt) {
+    const int nt1 = pp.nt[1], nt2 = pp.nt[2];
+    const int tt[3] = {(int)(tile / (nt1 * nt2)), (int)((tile / nt2) % nt1), (int)(tile % nt2)};
+    // per axis the options (tile, class): the own tile with every class, then
+    // the lower neighbour's particles reaching up (class 2) and the upper
+    // neighbour's reaching down (class 1); both from the same tile when nt = 2
+    int nopt[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) nopt[a] = pp.nt[a] == 1 ? 1 : 5;
+    const int ncomb = nopt[0] * nopt[1] * nopt[2];  // <= 125
+    b = 0;
+    cnt = 0;
+    if (q < ncomb) {
+        const int idx[3] = {q / (nopt[1] * nopt[2]), (q / nopt[2]) % nopt[1], q % nopt[2]};
+        int ot[3], oc[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int nt = pp.nt[a], x = idx[a];
+            if (x < 3) {
+                ot[a] = tt[a];
+                oc[a] = nt == 1 ? 0 : x;
             } else {
-                otile[a][k] = lo;  // lower tile, particles reaching up
-                ocls[a][k++] = 2;
-                otile[a][k] = hi;  // upper tile, particles reaching down
-                ocls[a][k++] = 1;
+                const int lo = (tt[a] + nt - 1) % nt, hi = (tt[a] + 1) % nt;
+                if (nt == 2) {
+                    ot[a] = hi;
+                    oc[a] = x == 3 ? 1 : 2;
+                } else {
+                    ot[a] = x == 3 ? lo : hi;
+                    oc[a] = x == 3 ? 2 : 1;
+                }
             }
         }
-        nopt[a] = k;
-    }
-    const int ncomb = nopt[0] * nopt[1] * nopt[2];  // <= 125
-    const int q = threadIdx.x;
-    uint32_t b = 0, cnt = 0;
-    if (q < ncomb) {
-        const int i = q / (nopt[1] * nopt[2]), j = (q / nopt[2]) % nopt[1], k = q % nopt[2];
-        const long key = (((long)otile[0][i] * nt1 + otile[1][j]) * nt2 + otile[2][k]) * 27 + ocls[0][i] * 9 +
-                         ocls[1][j] * 3 + ocls[2][k];
+        const long key = (((long)ot[0] * nt1 + ot[1]) * nt2 + ot[2]) * 27 + oc[0] * 9 + oc[1] * 3 + oc[2];
         b = off[key];
         cnt = off[key + 1] - b;
     }
-    uint32_t tot;
+    return ncomb;
+}
+
+// publish the fetched segments in shared memory (every thread takes part)
+__device__ void tile_publish(int ncomb, uint32_t b, uint32_t cnt, uint32_t *seg_begin, uint32_t *seg_pref,
+                             uint32_t *scan_ws, TileSegs &ts) {
+    const int q = threadIdx.x;
     const uint32_t pref = block_exclusive_scan(cnt, scan_ws, &scan_ws[31]);
-    tot = scan_ws[31];
+    const uint32_t tot = scan_ws[31];
     if (q < ncomb) {
         seg_begin[q] = b;
         seg_pref[q] = pref;
@@ -415,7 +433,15 @@ __device__ void tile_segments(const PaintParams &pp, const uint32_t *__restrict_
     if (q == 0) seg_pref[ncomb] = tot;
     __syncthreads();
     ts.nseg = ncomb;
-    ts.total = seg_pref[ncomb];
+    ts.total = tot;
+}
+
+__device__ void tile_segments(const PaintParams &pp, const uint32_t *__restrict__ off, uint32_t *seg_begin,
+                              uint32_t *seg_pref, uint32_t *scan_ws, TileSegs &ts) {
+    tile_geometry(pp, blockIdx.x, ts);
+    uint32_t b, cnt;
+    const int ncomb = tile_segment(pp, off, blockIdx.x, threadIdx.x, b, cnt);
+    tile_publish(ncomb, b, cnt, seg_begin, seg_pref, scan_ws, ts);
 }
 
 // index of particle q of the flattened segment list (largest segment whose
@@ -431,9 +457,10 @@ __device__ __forceinline__ uint32_t seg_index(uint32_t q, const uint32_t *seg_be
     return seg_begin[lo] + (q - seg_pref[lo]);
 }
 
-struct __align__(16) StageRec {
-    uint32_t loc[4];  // per axis: 4 packed local cell indices (255 = outside the tile); [3] unused
-    float4 w[3];      // per axis: PCS weights (k weights pre-scaled by 2^s)
+// per warp: the staged particles of one round, slot = particle + 16 * grid
+struct __align__(16) StageBuf {
+    uint4 loc[32];     // per axis: 4 packed local cell indices (255 = outside the tile); .w unused
+    float4 w[3][32];   // per axis: PCS weights (k weights pre-scaled by 2^s)
 };
 
 __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, uint32_t outv) {
@@ -449,228 +476,370 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, ui
     return r;
 }
 
-// deposit staged particles one at a time: lane = (grid, i row, j row), every
-// lane adds its row's 4 k cells.  By the bank layout the 32 rows of one
-// particle start in 32 distinct banks, so each of the 4 atomics is a single
-// shared-memory wavefront (the limiting resource of this kernel).  Cells
-// outside the tile land in the padding row / column.
+// deposit staged particles: lane = (grid, i row, j row), every lane adds its
+// row's 4 k cells.  By the bank layout each of the 4 atomic steps is a single
+// shared-memory wavefront.  Two particles are read before either is deposited
+// so the shared loads of one overlap the atomics of the other.  Stencil cells
+// outside the tile (local index kOut) are skipped.
+// slot of particle p of grid g in the stage buffer: the two grids' records
+// interleave so that lanes reading both fall in different banks
+__device__ __forceinline__ int stage_slot(int p, int g) { return 2 * p + g; }
+
 template <bool FIXED>
-__device__ __forceinline__ void deposit_all(uint32_t *acc, const StageRec *mystage, int np, int ngr, int lane) {
-    const int g = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
-    if (g >= ngr) return;
-    const float M = 12582912.0f;  // 1.5 * 2^23: FMA onto it rounds w to an integer
-    for (int p = 0; p < np; ++p) {
-        const StageRec &st = mystage[p * kMaxPaintGrids + g];
-        const uint4 loc = *reinterpret_cast<const uint4 *>(st.loc);
-        const uint32_t li = (loc.x >> (8 * a)) & 255u;
-        if (li == 255u) continue;
-        const uint32_t lj = (loc.y >> (8 * b)) & 255u;
-        uint32_t *row = acc + g * kGS + li * kSI + lj * kSJ;
-        const float w = reinterpret_cast<const float *>(&st.w[0])[a] * reinterpret_cast<const float *>(&st.w[1])[b];
-        const float4 wz = st.w[2];
-        const uint32_t k0 = loc.z & 255u, k1 = (loc.z >> 8) & 255u, k2 = (loc.z >> 16) & 255u, k3 = loc.z >> 24;
-        if (FIXED) {
-            atomicAdd(row + k0, __float_as_uint(fmaf(w, wz.x, M)) - 0x4B400000u);
-            atomicAdd(row + k1, __float_as_uint(fmaf(w, wz.y, M)) - 0x4B400000u);
-            atomicAdd(row + k2, __float_as_uint(fmaf(w, wz.z, M)) - 0x4B400000u);
-            atomicAdd(row + k3, __float_as_uint(fmaf(w, wz.w, M)) - 0x4B400000u);
-        } else {
-            float *rowf = reinterpret_cast<float *>(row);
-            atomicAdd(rowf + k0, w * wz.x);
-            atomicAdd(rowf + k1, w * wz.y);
-            atomicAdd(rowf + k2, w * wz.z);
-            atomicAdd(rowf + k3, w * wz.w);
-        }
+__device__ __forceinline__ void dep_one(uint32_t *cell, float w, float wz) {
+    if (FIXED) {
+        const float M = 12582912.0f;  // 1.5 * 2^23: FMA onto it rounds w * wz to an integer
+        atomicAdd(cell, __float_as_uint(fmaf(w, wz, M)) - 0x4B400000u);
+    } else {
+        atomicAdd(reinterpret_cast<float *>(cell), w * wz);
     }
 }
 
+// One particle of grid g for lane (a, b).
+// FAST (no tile spans a periodic axis): loc.x / loc.y are the offsets of the
+// particle's cells s ^ par for s = 0 and 1 in the stencil row (a, b) = (0, 0),
+// relative to the accumulator, with par the cell-order bit; row (a, b) adds
+// a*kSI + b*kSJ (lane_off).  loc.z has bit 4a + b set for the rows inside the
+// tile.  The 4 k cells are contiguous (kPadK columns take those beyond the tile).
+// Otherwise loc.x / loc.y hold the 4 local i / j indices as bytes (kOut outside
+// the tile) and loc.z the 4 padded k cells as bytes, in step order.
+// The k weights are stored in step order.
+template <bool FIXED, bool FAST>
+__device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, int slot, int g, int a, int b,
+                                            int lane_off) {
+    const uint4 loc = sb.loc[slot];
+    const float w = reinterpret_cast<const float *>(&sb.w[0][slot])[a] *
+                    reinterpret_cast<const float *>(&sb.w[1][slot])[b];
+    const float4 wz = sb.w[2][slot];
+    if (FAST) {
+        if (!((loc.z >> (4 * a + b)) & 1u)) return;  // a stencil row outside the tile
+        uint32_t *p0 = acc + (int)loc.x + lane_off;
+        uint32_t *p1 = acc + (int)loc.y + lane_off;
+        dep_one<FIXED>(p0, w, wz.x);
+        dep_one<FIXED>(p1, w, wz.y);
+        dep_one<FIXED>(p0 + 2, w, wz.z);
+        dep_one<FIXED>(p1 + 2, w, wz.w);
+    } else {
+        const uint32_t li = (loc.x >> (8 * a)) & 255u;
+        const uint32_t lj = (loc.y >> (8 * b)) & 255u;
+        if ((li | lj) >= 16u) return;
+        uint32_t *row = acc + g * kGS + li * kSI + lj * kSJ;
+        dep_one<FIXED>(row + (loc.z & 255u), w, wz.x);
+        dep_one<FIXED>(row + ((loc.z >> 8) & 255u), w, wz.y);
+        dep_one<FIXED>(row + ((loc.z >> 16) & 255u), w, wz.z);
+        dep_one<FIXED>(row + (loc.z >> 24), w, wz.w);
+    }
+}
+
+template <bool FIXED, bool FAST>
+__device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, int np, int ngr, int lane) {
+    const int g = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
+    if (g >= ngr) return;
+    const int lane_off = a * kSI + b * kSJ;
+#pragma unroll 2
+    for (int p = 0; p < np; ++p) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, g), g, a, b, lane_off);
+}
+
+// largest fixed-point exponent s for which `n` contributors to one cell cannot
+// overflow its 32-bit sum: each adds round(w 2^s) <= 8/27 2^s + 1/2 (the
+// largest PCS weight product is (2/3)^3), so n (16 2^s + 27) < 54 2^32 is
+// required.  Exact integer arithmetic; a negative result selects FP32 sums.
+__device__ __forceinline__ int fix_bits_for(uint32_t n) {
+    if (n == 0) return kMaxFixBits;
+    const unsigned long long x = (54ull << 32) / n;
+    if (x <= 28) return -1;
+    const unsigned long long q = (x - 28) >> 4;
+    const int fb = q == 0 ? -1 : 63 - __clzll((long long)q);
+    return fb > kMaxFixBits ? kMaxFixBits : fb;
+}
+
+// Persistent: each CTA paints tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// The next tile's segment offsets are loaded during the write-out, the
+// accumulators are cleared as they are written out, and each warp loads its
+// next batch of records before depositing the current one.
 __global__ void __launch_bounds__(kPaintThreads, 2)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
-                  PaintOut po) {
+                  PaintOut po, unsigned ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                       // [2][kGS]
-    StageRec *stage = reinterpret_cast<StageRec *>(acc + kMaxPaintGrids * kGS);  // [warps][16][grids]
-    uint32_t *blk = reinterpret_cast<uint32_t *>(stage + (kPaintThreads / 32) * kStageParts * kMaxPaintGrids);  // [kBlkN]
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                 // [2][kGS]
+    StageBuf *stage = reinterpret_cast<StageBuf *>(smem_raw + kAccBytes);  // [warps]
+    uint32_t *blk = reinterpret_cast<uint32_t *>(stage + kPaintThreads / 32);  // [kBlkN]
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
     __shared__ uint32_t scan_ws[32];
     __shared__ int fixbits_s;
+    // packed local indices of the 4 stencil cells along i and j for a first
+    // cell at l = -4 .. 35 relative to the tile start (kOut outside the tile);
+    // they depend only on the tile extent, so they are rebuilt only when it changes
+    __shared__ uint32_t loctab[2][40];
+    // and as row masks: bit a (one bit per nibble for i, for the product with
+    // the j mask) set when stencil row a lies inside the tile
+    __shared__ uint32_t masktab[2][40];
+    int tab_te0 = -1, tab_te1 = -1;
 
     const int Ng = pp.Ng, ngr = pp.ngrids;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    for (int e = tid; e < ngr * kGS / 4; e += blockDim.x) reinterpret_cast<uint4 *>(acc)[e] = make_uint4(0, 0, 0, 0);
-    for (int e = tid; e < kBlkN; e += blockDim.x) blk[e] = 0u;
+    unsigned tile = blockIdx.x;
+    if (tile >= ntiles) return;
+    for (int e = tid; e < (int)(kAccBytes / 16); e += blockDim.x)
+        reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
     TileSegs ts;
-    tile_segments(pp, off, seg_begin, seg_pref, scan_ws, ts);
-    const uint32_t total = ts.total;
-    const int nseg = ts.nseg;
-
-    // pass A: particles per 4^3 block of grid-0 base cells.  Along an axis cut
-    // into several tiles the blocks cover the tile plus a 4-cell margin; along
-    // an axis held by a single tile they tile the periodic axis itself.
-    int nb[3];
-    bool cyc[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        cyc[a] = ts.te[a] == Ng;
-        nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
+    {
+        uint32_t b, cnt;
+        const int ncomb = tile_segment(pp, off, tile, tid, b, cnt);
+        tile_publish(ncomb, b, cnt, seg_begin, seg_pref, scan_ws, ts);  // also orders the clearing above
     }
     const int fb = pp.fb;
-    for (uint32_t q = tid; q < total; q += blockDim.x) {
-        const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
-        const uint32_t rw[3] = {r.x, r.y, r.z};
-        int bidx = 0;
+    for (;;) {
+        tile_geometry(pp, tile, ts);
+        const uint32_t total = ts.total;
+        const int nseg = ts.nseg;
+        bool cyc[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int b = (int)(rw[a] >> fb);
-            int bb;
-            if (cyc[a]) {
-                bb = b / kBlk;
-            } else {
-                int l = b - ts.t0[a];
-                if (l > Ng / 2) l -= Ng;
-                if (l < -Ng / 2) l += Ng;
-                bb = (l + 4) / kBlk;  // margin of 4 cells below the tile
-                bb = bb < 0 ? 0 : (bb >= nb[a] ? nb[a] - 1 : bb);
-            }
-            bidx = bidx * blk_dim(a) + bb;
-        }
-        atomicAdd(&blk[bidx], 1u);
-    }
-    __syncthreads();
-    // A cell's contributors have grid-0 base cells from 3 below to 3 above it
-    // per axis, within 3 consecutive blocks (cyclically on a periodic axis):
-    // the largest 3x3x3 block sum bounds every cell's contributor count.
-    // Separable window sums along k, then j, then i; tmp reuses the stage area.
-    {
-        uint32_t *tmp = reinterpret_cast<uint32_t *>(stage);
-        const int D1 = blk_dim(1), D2 = blk_dim(2);
-        for (int e = tid; e < kBlkN; e += blockDim.x) {
-            const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
-            uint32_t v = 0;
-            const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[2] || k + 2 < nb[2]);
-            if (in)
-                for (int c = 0; c < 3; ++c) v += blk[(i * D1 + j) * D2 + (cyc[2] ? (k + c) % nb[2] : k + c)];
-            tmp[e] = v;
-        }
-        __syncthreads();
-        for (int e = tid; e < kBlkN; e += blockDim.x) {
-            const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
-            uint32_t v = 0;
-            const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[1] || j + 2 < nb[1]);
-            if (in)
-                for (int c = 0; c < 3; ++c) v += tmp[(i * D1 + (cyc[1] ? (j + c) % nb[1] : j + c)) * D2 + k];
-            blk[e] = v;
-        }
-        __syncthreads();
-        uint32_t mx = 0;
-        for (int e = tid; e < kBlkN; e += blockDim.x) {
-            const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
-            const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[0] || i + 2 < nb[0]);
-            if (in) {
-                uint32_t v = 0;
-                for (int c = 0; c < 3; ++c) v += blk[((cyc[0] ? (i + c) % nb[0] : i + c) * D1 + j) * D2 + k];
-                mx = max(mx, v);
-            }
-        }
+        for (int a = 0; a < 3; ++a) cyc[a] = ts.te[a] == Ng;
+        if (ts.te[0] != tab_te0 || ts.te[1] != tab_te1) {
+            if (tid < 80) {
+                const int a = tid / 40, l = tid % 40 - 4, te = ts.te[a];
+                uint32_t v = 0, m = 0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) scan_ws[warp] = mx;
-        __syncthreads();
-        if (tid == 0) {
-            uint32_t m = 0;
-            for (int w = 0; w < nwarp; ++w) m = max(m, scan_ws[w]);
-            int fb = kMaxFixBits;
-            if (m > 0) fb = (int)floor(log2(4294967295.0 / ((double)m * kMaxCellWeight)));
-            fixbits_s = fb > kMaxFixBits ? kMaxFixBits : fb;
+                for (int s4 = 0; s4 < 4; ++s4) {
+                    const bool in = (unsigned)(l + s4) < (unsigned)te;
+                    v |= (in ? (uint32_t)(l + s4) : kOut) << (8 * s4);
+                    m |= (in ? 1u : 0u) << (a == 0 ? 4 * s4 : s4);
+                }
+                loctab[a][l + 4] = v;
+                masktab[a][l + 4] = m;
+            }
+            __syncthreads();
+            tab_te0 = ts.te[0];
+            tab_te1 = ts.te[1];
         }
-    }
-    __syncthreads();
-    const int fixbits = fixbits_s;
-    const bool fixed = fixbits >= kMinFixBits;
-    const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
 
-    // pass B: stage 32 particles per warp, then deposit them one by one
-    StageRec *mystage = stage + warp * kStageParts * kMaxPaintGrids;
-    for (uint32_t base = (uint32_t)warp * kStageParts; base < total; base += (uint32_t)nwarp * kStageParts) {
-        const uint32_t q = base + (lane & (kStageParts - 1));
-        const int gs = lane / kStageParts;  // lanes 0..15 stage grid 0, 16..31 grid 1
-        if (q < total && gs < ngr) {
-            const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
-            const uint32_t rw[3] = {r.x, r.y, r.z};
-            StageRec &st = mystage[(lane & (kStageParts - 1)) * kMaxPaintGrids + gs];
-            const float inv = ldexpf(1.0f, -fb);
+        // fixed-point scale: the tile's particle total bounds every cell's
+        // contributor count; only when that bound costs precision are the
+        // particles counted per 4^3 block of grid-0 base cells (over the tile
+        // plus a 4-cell margin, or the whole periodic axis when one tile spans it)
+        int fixbits = fix_bits_for(total);
+        if (fixbits < kMaxFixBits) {
+            int nb[3];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                int bg;
-                uint32_t dgq;
-                cell_g((int)(rw[a] >> fb), rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
-                float w[4];
-                pcs_weights((float)dgq * inv, w);
-                const uint32_t outv = a == 0 ? 255u : (a == 1 ? kOutJ : kOutK);
-                uint32_t loc;
-                if (cyc[a]) {
-                    loc = pack_local(bg, Ng, ts.t0[a], ts.te[a], outv);
-                } else {
-                    // linear local index of the first stencil cell (periodic
-                    // images folded to the nearest copy of the tile)
+            for (int a = 0; a < 3; ++a) nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
+            for (int e = tid; e < kBlkN; e += blockDim.x) blk[e] = 0u;
+            __syncthreads();
+            for (uint32_t q = tid; q < total; q += blockDim.x) {
+                const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+                const uint32_t rw[3] = {r.x, r.y, r.z};
+                int bidx = 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const int b = (int)(rw[a] >> fb);
+                    int bb;
+                    if (cyc[a]) {
+                        bb = b / kBlk;
+                    } else {
+                        int l = b - ts.t0[a];
+                        if (l > Ng / 2) l -= Ng;
+                        if (l < -Ng / 2) l += Ng;
+                        bb = (l + 4) / kBlk;  // margin of 4 cells below the tile
+                        bb = bb < 0 ? 0 : (bb >= nb[a] ? nb[a] - 1 : bb);
+                    }
+                    bidx = bidx * blk_dim(a) + bb;
+                }
+                atomicAdd(&blk[bidx], 1u);
+            }
+            __syncthreads();
+            // A cell's contributors have grid-0 base cells from 3 below to 3
+            // above it per axis, within 3 consecutive blocks (cyclically on a
+            // periodic axis): the largest 3x3x3 block sum bounds every cell's
+            // contributor count.  Separable window sums along k, j, i; tmp
+            // reuses the stage area.
+            uint32_t *tmp = reinterpret_cast<uint32_t *>(stage);
+            const int D1 = blk_dim(1), D2 = blk_dim(2);
+            for (int e = tid; e < kBlkN; e += blockDim.x) {
+                const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
+                uint32_t v = 0;
+                const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[2] || k + 2 < nb[2]);
+                if (in)
+                    for (int c = 0; c < 3; ++c) v += blk[(i * D1 + j) * D2 + (cyc[2] ? (k + c) % nb[2] : k + c)];
+                tmp[e] = v;
+            }
+            __syncthreads();
+            for (int e = tid; e < kBlkN; e += blockDim.x) {
+                const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
+                uint32_t v = 0;
+                const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[1] || j + 2 < nb[1]);
+                if (in)
+                    for (int c = 0; c < 3; ++c) v += tmp[(i * D1 + (cyc[1] ? (j + c) % nb[1] : j + c)) * D2 + k];
+                blk[e] = v;
+            }
+            __syncthreads();
+            uint32_t mx = 0;
+            for (int e = tid; e < kBlkN; e += blockDim.x) {
+                const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
+                const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[0] || i + 2 < nb[0]);
+                if (in) {
+                    uint32_t v = 0;
+                    for (int c = 0; c < 3; ++c) v += blk[((cyc[0] ? (i + c) % nb[0] : i + c) * D1 + j) * D2 + k];
+                    mx = max(mx, v);
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane == 0) scan_ws[warp] = mx;
+            __syncthreads();
+            if (tid == 0) {
+                uint32_t m = 0;
+                for (int w = 0; w < nwarp; ++w) m = max(m, scan_ws[w]);
+                fixbits_s = fix_bits_for(m);
+            }
+            __syncthreads();
+            fixbits = fixbits_s;
+        }
+        const bool fixed = fixbits >= kMinFixBits;
+        const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
+
+        // pass B: each warp stages 16 particles (both grids), then deposits
+        // them one by one; the records of the warp's next batch are loaded
+        // before the deposit so their latency hides behind it
+        StageBuf &sb = stage[warp];
+        const bool fast = !(cyc[0] || cyc[1] || cyc[2]);
+        const int gs = lane / kStageParts;  // lanes 0..15 stage grid 0, 16..31 grid 1
+        const uint32_t bstride = (uint32_t)nwarp * kStageParts;
+        uint32_t base = (uint32_t)warp * kStageParts;
+        uint4 rec = make_uint4(0, 0, 0, 0);
+        {
+            const uint32_t q = base + (lane & (kStageParts - 1));
+            if (q < total && gs < ngr) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+        }
+        for (; base < total; base += bstride) {
+            const uint32_t q = base + (lane & (kStageParts - 1));
+            if (q < total && gs < ngr) {
+                const uint32_t rw[3] = {rec.x, rec.y, rec.z};
+                const float inv = ldexpf(1.0f, -fb);
+                const int slot = stage_slot(lane & (kStageParts - 1), gs);
+                int bgv[3], lv[3];
+                uint32_t par = 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const int b0 = (int)(rw[a] >> fb);
+                    int bg;
+                    uint32_t dgq;
+                    cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
+                    float w[4];
+                    pcs_weights((float)dgq * inv, w);
+                    float4 wv = make_float4(w[0], w[1], w[2], w[3]);
+                    if (a == 2) {
+                        wv = make_float4(wv.x * fscale, wv.y * fscale, wv.z * fscale, wv.w * fscale);
+                        par = (uint32_t)(bg - b0) & 1u;
+                        if (par) wv = make_float4(wv.y, wv.x, wv.w, wv.z);  // k cells in the order s ^ 1
+                    }
+                    sb.w[a][slot] = wv;
+                    // local index of the first stencil cell (periodic images
+                    // folded to the nearest copy of the tile)
                     int l = bg - 1 - ts.t0[a];
                     l -= l > Ng / 2 ? Ng : 0;
                     l += l < -Ng / 2 ? Ng : 0;
-                    loc = 0;
-#pragma unroll
-                    for (int s4 = 0; s4 < 4; ++s4)
-                        loc |= ((unsigned)(l + s4) < (unsigned)ts.te[a] ? (uint32_t)(l + s4) : outv) << (8 * s4);
+                    bgv[a] = bg;
+                    lv[a] = l;
                 }
-                st.loc[a] = loc;
-                const float sc = a == 2 ? fscale : 1.f;
-                st.w[a] = make_float4(w[0] * sc, w[1] * sc, w[2] * sc, w[3] * sc);
+                const bool kmiss = !cyc[2] && (lv[2] < -3 || lv[2] >= ts.te[2]);  // stencil misses the tile
+                uint4 loc;
+                if (fast) {
+                    const uint32_t mi = (unsigned)(lv[0] + 4) < 40u ? masktab[0][lv[0] + 4] : 0u;
+                    const uint32_t mj = (unsigned)(lv[1] + 4) < 40u ? masktab[1][lv[1] + 4] : 0u;
+                    const int b0 = gs * kGS + lv[0] * kSI + lv[1] * kSJ + lv[2] + kPadK + (int)par;
+                    loc = make_uint4((uint32_t)b0, (uint32_t)(b0 + 1 - 2 * (int)par), kmiss ? 0u : mi * mj, 0u);
+                } else {
+                    uint32_t li, lj, lk;
+                    li = cyc[0] ? pack_local(bgv[0], Ng, ts.t0[0], ts.te[0], kOut)
+                                : ((unsigned)(lv[0] + 4) < 40u ? loctab[0][lv[0] + 4] : 0xFFFFFFFFu);
+                    lj = cyc[1] ? pack_local(bgv[1], Ng, ts.t0[1], ts.te[1], kOut)
+                                : ((unsigned)(lv[1] + 4) < 40u ? loctab[1][lv[1] + 4] : 0xFFFFFFFFu);
+                    if (cyc[2])
+                        lk = pack_local(bgv[2], Ng, ts.t0[2], ts.te[2], 0u) + 0x01010101u * kPadK;
+                    else
+                        lk = (uint32_t)(kmiss ? 0 : lv[2] + kPadK) * 0x01010101u + 0x03020100u;
+                    if (par) lk = ((lk & 0x00FF00FFu) << 8) | ((lk >> 8) & 0x00FF00FFu);
+                    loc = make_uint4(kmiss ? 0xFFFFFFFFu : li, lj, lk, 0u);
+                }
+                sb.loc[slot] = loc;
             }
+            __syncwarp();
+            {
+                const uint32_t qn = base + bstride + (lane & (kStageParts - 1));
+                if (qn < total && gs < ngr) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
+            }
+            const int np = min((uint32_t)kStageParts, total - base);
+            if (fast) {
+                if (fixed)
+                    deposit_all<true, true>(acc, sb, np, ngr, lane);
+                else
+                    deposit_all<false, true>(acc, sb, np, ngr, lane);
+            } else {
+                if (fixed)
+                    deposit_all<true, false>(acc, sb, np, ngr, lane);
+                else
+                    deposit_all<false, false>(acc, sb, np, ngr, lane);
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        const int np = min((uint32_t)kStageParts, total - base);
-        if (fixed)
-            deposit_all<true>(acc, mystage, np, ngr, lane);
-        else
-            deposit_all<false>(acc, mystage, np, ngr, lane);
-        __syncwarp();
-    }
-    __syncthreads();
+        __syncthreads();
 
-    // write the owned cells (and the row padding of the last k tile): one
-    // warp per (i, j) row, lanes along k, rows advanced incrementally
-    const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
-    const int pad = last_k ? pp.Ng_pad - Ng : 0;
-    const int rowlen = ts.te[2] + pad, te1 = ts.te[1], te2 = ts.te[2];
-    const int nrow = ts.te[0] * te1;
-    const long rstride = (long)pp.Ng_pad;  // global floats between consecutive j
-    for (int g = 0; g < ngr; ++g) {
-        float *out = reinterpret_cast<float *>(po.out[g]) + ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
-        const float sc = (float)ldexp(po.scale[g], fixed ? -fixbits : 0);
-        const bool accu = po.accumulate[g] != 0;
-        int li = warp / te1, lj = warp - li * te1;
-        const int dli = nwarp / te1, dlj = nwarp - dli * te1;
-        for (int r = warp; r < nrow; r += nwarp) {
-            float *orow = out + ((long)li * Ng + lj) * rstride;
-            const uint32_t *arow = acc + g * kGS + li * kSI + lj * kSJ;
-            for (int lk = lane; lk < rowlen; lk += 32) {
-                float v = 0.f;
-                if (lk < te2) {
-                    const uint32_t a = arow[lk];
-                    v = (fixed ? __uint2float_rn(a) : __uint_as_float(a)) * sc;
+        // the next tile's segments, loaded now and published after the write-out
+        const unsigned next = tile + gridDim.x;
+        uint32_t nb_begin = 0, nb_cnt = 0;
+        int nb_comb = 0;
+        if (next < ntiles) nb_comb = tile_segment(pp, off, next, tid, nb_begin, nb_cnt);
+
+        // write the owned cells (and the row padding of the last k tile),
+        // clearing them for the next tile: warp w writes the i rows w, w + 16,
+        // ..., stepping along j with pointer increments; lanes along k
+        {
+            const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
+            const int rowlen = ts.te[2] + (last_k ? pp.Ng_pad - Ng : 0);
+            const int te1 = ts.te[1], te2 = ts.te[2];
+            const long rstride = (long)pp.Ng_pad;  // global floats between consecutive j
+            const long istride = rstride * Ng;     // and between consecutive i
+            const float sc0 = (float)ldexp(po.scale[0], fixed ? -fixbits : 0);
+            const float sc1 = ngr > 1 ? (float)ldexp(po.scale[1], fixed ? -fixbits : 0) : 0.f;
+            const long obase = ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
+            for (int li = warp; li < ts.te[0]; li += nwarp) {
+                float *o0 = reinterpret_cast<float *>(po.out[0]) + obase + li * istride;
+                float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
+                uint32_t *a0 = acc + kPadK + li * kSI;
+                uint32_t *a1 = a0 + kGS;
+                for (int lj = 0; lj < te1; ++lj, o0 += rstride, o1 += rstride, a0 += kSJ, a1 += kSJ) {
+                    float v0 = 0.f, v1 = 0.f;
+                    if (lane < te2) {
+                        const uint32_t c0 = a0[lane];
+                        a0[lane] = 0u;
+                        v0 = (fixed ? __uint2float_rn(c0) : __uint_as_float(c0)) * sc0;
+                        if (ngr > 1) {
+                            const uint32_t c1 = a1[lane];
+                            a1[lane] = 0u;
+                            v1 = (fixed ? __uint2float_rn(c1) : __uint_as_float(c1)) * sc1;
+                        }
+                    }
+                    if (lane < rowlen) {
+                        if (!po.accumulate[0]) o0[lane] = v0;
+                        else if (lane < te2) o0[lane] += v0;
+                        if (ngr > 1) {
+                            if (!po.accumulate[1]) o1[lane] = v1;
+                            else if (lane < te2) o1[lane] += v1;
+                        }
+                    }
+                    if (lane + 32 < rowlen) {  // row padding beyond a full 32-cell tile
+                        if (!po.accumulate[0]) o0[lane + 32] = 0.f;
+                        if (ngr > 1 && !po.accumulate[1]) o1[lane + 32] = 0.f;
+                    }
                 }
-                if (!accu)
-                    orow[lk] = v;
-                else if (lk < te2)
-                    orow[lk] += v;
-            }
-            li += dli;
-            lj += dlj;
-            if (lj >= te1) {
-                lj -= te1;
-                ++li;
             }
         }
+        if (next >= ntiles) break;
+        // the clearing above completes before the next deposit: tile_publish
+        // synchronises the CTA
+        tile_publish(nb_comb, nb_begin, nb_cnt, seg_begin, seg_pref, scan_ws, ts);
+        tile = next;
     }
 }
 
@@ -885,11 +1054,11 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
-        const size_t smem = sizeof(uint32_t) * kMaxPaintGrids * kGS +
-                            sizeof(StageRec) * (kPaintThreads / 32) * kStageParts * kMaxPaintGrids +
-                            sizeof(uint32_t) * kBlkN;
+        const size_t smem = kAccBytes + sizeof(StageBuf) * (kPaintThreads / 32) + sizeof(uint32_t) * kBlkN;
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        paint_coop_kernel<<<ntiles, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po);
+        unsigned nb = (unsigned)(2 * num_sms());
+        nb = nb < ntiles ? nb : ntiles;
+        paint_coop_kernel<<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
     } else {
         const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
         FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
