@@ -180,47 +180,50 @@ template <> struct Rec<double> { struct type { double x, y, z; }; };
 // ---- 1. key + histogram -------------------------------------------------------
 
 template <typename P>
+__device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintParams &pp) {
+    const int Ng = pp.Ng;
+    int t[3], cls[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int b0;
+        uint32_t dq0 = 0;
+        if constexpr (sizeof(P) == 4) {
+            cell0(pos[a], pp.ax[a], Ng, pp.fb, b0, dq0);
+        } else {
+            P d;
+            coord(pos[a], pp.ax[a], 0, Ng, b0, d);
+        }
+        const int ta = pp.tile_of[a][b0];
+        const int t0 = pp.start[a][ta];
+        const int te = pp.start[a][ta + 1] - t0;
+        int rmin = b0 - t0, rmax = b0 - t0;
+        for (int g = 1; g < pp.ngrids; ++g) {
+            int bg;
+            if constexpr (sizeof(P) == 4) {
+                uint32_t dgq;
+                cell_g(b0, dq0, pp.ax[a].dq[g], pp.fb, Ng, bg, dgq);
+            } else {
+                P dg;
+                coord(pos[a], pp.ax[a], g, Ng, bg, dg);
+            }
+            const int dl = ((bg - b0 + Ng + 1) % Ng) - 1;  // -1, 0 or +1
+            rmin = min(rmin, b0 - t0 + dl);
+            rmax = max(rmax, b0 - t0 + dl);
+        }
+        t[a] = ta;
+        cls[a] = pp.nt[a] == 1 ? 0 : (rmin - 1 < 0 ? 1 : (rmax + 2 >= te ? 2 : 0));
+    }
+    return (uint32_t)((((long)t[0] * pp.nt[1] + t[1]) * pp.nt[2] + t[2]) * 27 + cls[0] * 9 + cls[1] * 3 + cls[2]);
+}
+
+template <typename P>
 __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ y,
                                  const P *__restrict__ z, long Np, PaintParams pp,
                                  uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                                  uint32_t *__restrict__ hist) {
-    const int Ng = pp.Ng;
-    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np;
-         p += (long)gridDim.x * blockDim.x) {
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
         const P pos[3] = {x[p], y[p], z[p]};
-        int t[3], cls[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            int b0;
-            uint32_t dq0 = 0;
-            if constexpr (sizeof(P) == 4) {
-                cell0(pos[a], pp.ax[a], Ng, pp.fb, b0, dq0);
-            } else {
-                P d;
-                coord(pos[a], pp.ax[a], 0, Ng, b0, d);
-            }
-            const int ta = pp.tile_of[a][b0];
-            const int t0 = pp.start[a][ta];
-            const int te = pp.start[a][ta + 1] - t0;
-            int rmin = b0 - t0, rmax = b0 - t0;
-            for (int g = 1; g < pp.ngrids; ++g) {
-                int bg;
-                if constexpr (sizeof(P) == 4) {
-                    uint32_t dgq;
-                    cell_g(b0, dq0, pp.ax[a].dq[g], pp.fb, Ng, bg, dgq);
-                } else {
-                    P dg;
-                    coord(pos[a], pp.ax[a], g, Ng, bg, dg);
-                }
-                const int dl = ((bg - b0 + Ng + 1) % Ng) - 1;  // -1, 0 or +1
-                rmin = min(rmin, b0 - t0 + dl);
-                rmax = max(rmax, b0 - t0 + dl);
-            }
-            t[a] = ta;
-            cls[a] = pp.nt[a] == 1 ? 0 : (rmin - 1 < 0 ? 1 : (rmax + 2 >= te ? 2 : 0));
-        }
-        const uint32_t k = (uint32_t)((((long)t[0] * pp.nt[1] + t[1]) * pp.nt[2] + t[2]) * 27 + cls[0] * 9 +
-                                      cls[1] * 3 + cls[2]);
+        const uint32_t k = paint_key_of<P>(pos, pp);
         key[p] = k;
         rank[p] = atomicAdd(&hist[k], 1u);
     }
@@ -323,8 +326,7 @@ __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restric
                                      const uint32_t *__restrict__ rank,
                                      const uint32_t *__restrict__ off,
                                      typename Rec<P>::type *__restrict__ sorted) {
-    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np;
-         p += (long)gridDim.x * blockDim.x) {
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
         const uint32_t dst = off[key[p]] + rank[p];
         typename Rec<P>::type r;
         if constexpr (sizeof(P) == 4) {
