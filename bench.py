@@ -317,13 +317,15 @@ def run_ours(args):
     kern = {k: avg[k] for k in algo if k != "upload"}
     dom = max(kern, key=kern.get)
     achieved = algo[dom] / (avg[dom] / 1000.0) / 1e9
+    # DRAM bytes per launch of each kernel at this workload, from an ncu capture
+    # (profiles/traffic_ng1024_np1e8.txt, "stage bytes" lines)
     traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tr_path):
-        try:
-            traffic = json.load(open(tr_path)).get(dom)
-        except Exception:
-            traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic_ng1024_np1e8.txt")
+    if Ng == NG and Np == int(NP) and os.path.exists(tr_path):
+        for line in open(tr_path):
+            f = line.split("#")[0].split()
+            if len(f) == 2 and f[0] == dom:
+                traffic = int(f[1])
     # whole-step algorithmic bytes of the unfused pipeline: paint 12 Np + 2 G,
     # FFT 2 HBM passes (R+W) per grid, phase/average/deconv 3 G, binning G
     G4 = Ng * Ng * 2 * (Ng // 2 + 1) * 4
