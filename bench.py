@@ -197,13 +197,19 @@ def run_reference(args):
 
 # ---------------------------------------------------------------------------
 def make_catalog(torch, Np: int, seed: int, mock: str, dev):
-    g = torch.Generator(device=dev)
-    g.manual_seed(seed)
+    """(3, N) FP32 positions on the device: a uniform box, or a lognormal
+    mock (256^3 field, Zel'dovich velocities, redshift space along z) with
+    about Np particles."""
     if mock == "uniform":
-        pos = torch.rand((3, Np), generator=g, device=dev, dtype=torch.float32) * L_BOX
-        return pos
-    from fftgal_gb300 import mocks
-    return mocks.lognormal_rsd_catalog(torch, Np, L_BOX, seed=seed, device=dev)
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        return torch.rand((3, Np), generator=g, device=dev, dtype=torch.float32) * L_BOX
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from lognormal import lognormal_catalog
+    x, y, z, vx, vy, vz = lognormal_catalog(seed, 256, L_BOX, Np)
+    pos = np.stack([x, y, z + vz]).astype(np.float32)  # gal_rsd along z with aH = 1
+    return torch.from_numpy(pos).to(dev)
 
 
 def algorithmic_bytes(Ng: int, Np: int):
@@ -243,6 +249,7 @@ def run_ours(args):
     V = L_BOX ** 3
 
     pos = make_catalog(torch, Np, 1234 + rank, args.mock, dev)
+    Np = int(pos.shape[1])
     grid = fg.Grid(Ng, L_BOX, precision="f32", host_view="lazy")
     grid.set_stream(stream.cuda_stream)
     xp, yp, zp = (pos[a].data_ptr() for a in range(3))
@@ -346,7 +353,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "catalogs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": f"synthetic ({args.mock}, seeded, generated on the GPU)",
+            "data": ("synthetic (uniform, seeded, generated on the GPU)" if args.mock == "uniform" else
+                     "synthetic (lognormal mock with z-RSD, seeded, numpy)"),
             "config": {"workload": f"interlaced PCS P_l (l=0,2,4,6) + {NMU} mu-wedges, Ng={Ng}, Np={Np:.0e}, "
                                    f"L={L_BOX:g}, dK=2pi/L, FP32 positions+grids, FP64 bin sums",
                        "Ng": Ng, "Np": Np, "los": LOS, "mock": args.mock,
