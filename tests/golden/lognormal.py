@@ -33,7 +33,7 @@ def lognormal_catalog(seed: int, n: int, L: float, Np: float, f: float = 0.8):
     w = rng.standard_normal((n, n, n))
     gk = np.fft.rfftn(w) * np.sqrt(pk_model(kk) * n ** 3 / L ** 3)
     gk[0, 0, 0] = 0.0
-    g = np.fft.irfftn(gk, s=(n, n, n))
+    g = np.fft.irfftn(gk, s=(n, n, n), axes=(0, 1, 2))
     sig2 = g.var()
     dln = np.exp(g - 0.5 * sig2) - 1.0
     nbar_cell = Np / n ** 3
@@ -50,6 +50,6 @@ def lognormal_catalog(seed: int, n: int, L: float, Np: float, f: float = 0.8):
         inv = np.where(k2 > 0, 1.0 / k2, 0.0)
     vel = []
     for kc in (kx, ky, kzz):
-        psi = np.fft.irfftn(1j * kc * inv * gk, s=(n, n, n))
+        psi = np.fft.irfftn(1j * kc * inv * gk, s=(n, n, n), axes=(0, 1, 2))
         vel.append(f * psi.ravel()[cell])
     return x, y, z, vel[0], vel[1], vel[2]
