@@ -300,13 +300,13 @@ def run_ours(args):
     host = torch.empty((3, Np), dtype=torch.float32, pin_memory=True)
     host.copy_(pos)
     hp = [host[a].numpy() for a in range(3)]
-    for _ in range(2):
-        grid.power_f32(hp[0], hp[1], hp[2], V, LOS, dK, Nmu=NMU)
+    # fftgal_power_batch_f32: one catalog per step, each copied host -> device
+    # inside the timed region (overlapping the previous catalog's computation)
+    grid.power_batch_f32([hp] * 2, V, LOS, dK, Nmu=NMU)
     barrier()
     k2 = max(3, args.steps // 2)
     e0.record(stream)
-    for _ in range(k2):
-        grid.power_f32(hp[0], hp[1], hp[2], V, LOS, dK, Nmu=NMU)
+    grid.power_batch_f32([hp] * k2, V, LOS, dK, Nmu=NMU)
     e1.record(stream)
     barrier()
     ms2 = e0.elapsed_time(e1)

@@ -92,6 +92,11 @@ SIGNATURES = {
     "fftgal_nk": (C.c_int, [C.c_int, C.c_double, C.c_double]),
     "fftgal_power_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                    C.c_int, _dp, C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
+    "fftgal_power_batch_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp, _dp,
+                                         C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
+    "fftgal_power_rsd_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_long, C.c_double, C.c_int, _dp, C.c_double, C.c_double,
+                                       C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_set_timing": (C.c_int, [_P_F, C.c_int]),
     "fftgal_stage_times": (C.c_int, [_P_F, _dp]),
     "fftgal_g2p_sum": (C.c_int, [_P_F, _P_G, _dp]),
@@ -339,6 +344,53 @@ class Grid:
                                       l.ctypes.data_as(_dp), float(dK), int(Nmu),
                                       K.ctypes.data_as(_dp), N.ctypes.data_as(_lp), P.ctypes.data_as(_dp),
                                       Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))
+        return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm)
+
+    def power_batch_f32(self, cats, V, los, dK: float, Nmu: int = 3) -> list:
+        """fftgal_power_f32 of every (x, y, z) host catalog in ``cats`` (V: one
+        volume per catalog), uploads overlapped with the computation.  Arrays
+        that are FP32 and C-contiguous (ideally page-locked) are used in place."""
+        arrs = [[np.ascontiguousarray(a, dtype=np.float32) for a in c] for c in cats]
+        n = len(arrs)
+        ptr = [(C.c_void_p * n)(*[c[a].ctypes.data for c in arrs]) for a in range(3)]
+        Np = np.array([len(c[0]) for c in arrs], dtype=np.int64)
+        Vs = np.ascontiguousarray(np.broadcast_to(np.asarray(V, dtype=np.float64), (n,)))
+        NK = lib().fftgal_nk(self.Ng, self.L, float(dK))
+        K = np.zeros((n, NK))
+        N = np.zeros((n, NK), dtype=np.int64)
+        P = np.zeros((n, NK, 4))
+        Km = np.zeros((n, NK, Nmu))
+        Nm = np.zeros((n, NK, Nmu), dtype=np.int64)
+        Pm = np.zeros((n, NK, Nmu))
+        l = _f64(los)
+        _check(lib().fftgal_power_batch_f32(self.p, n, ptr[0], ptr[1], ptr[2], Np.ctypes.data_as(_lp),
+                                            Vs.ctypes.data_as(_dp), l.ctypes.data_as(_dp), float(dK), int(Nmu),
+                                            K.ctypes.data_as(_dp), N.ctypes.data_as(_lp), P.ctypes.data_as(_dp),
+                                            Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))
+        return [dict(K=K[c], N=N[c], P=P[c], Kmu=Km[c], Nmu=Nm[c], Pmu=Pm[c]) for c in range(n)]
+
+    def power_rsd_f32(self, x, y, z, vx, vy, vz, V: float, los, aH: float, dK: float, Nmu: int = 3,
+                      where: int = MEM_HOST, Np: int | None = None) -> dict:
+        """power_f32 of the catalog displaced along ``los`` by (v . los)/aH
+        (gal_rsd fused into the paint)."""
+        if where == MEM_HOST:
+            arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, vx, vy, vz)]
+            ptrs = [a.ctypes.data for a in arrs]
+            Np = len(arrs[0])
+        else:
+            ptrs = [int(a) for a in (x, y, z, vx, vy, vz)]
+        NK = lib().fftgal_nk(self.Ng, self.L, float(dK))
+        K = np.zeros(NK)
+        N = np.zeros(NK, dtype=np.int64)
+        P = np.zeros((NK, 4))
+        Km = np.zeros((NK, Nmu))
+        Nm = np.zeros((NK, Nmu), dtype=np.int64)
+        Pm = np.zeros((NK, Nmu))
+        l = _f64(los)
+        _check(lib().fftgal_power_rsd_f32(self.p, *ptrs, int(Np), float(V), int(where), l.ctypes.data_as(_dp),
+                                          float(aH), float(dK), int(Nmu), K.ctypes.data_as(_dp),
+                                          N.ctypes.data_as(_lp), P.ctypes.data_as(_dp), Km.ctypes.data_as(_dp),
+                                          Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))
         return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm)
 
 

@@ -89,6 +89,12 @@ struct Grid {
     PaintScratch scratch;
     void *d_pos = nullptr;  // 3 position arrays (float or double)
     size_t pos_cap = 0;     // bytes
+    // fftgal_power_batch_f32: two device buffers of FP32 positions (one being
+    // uploaded on copy_stream while the other is painted) and their events
+    float *d_batch[2] = {nullptr, nullptr};
+    size_t batch_cap = 0;  // floats per buffer
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t up_done[2] = {nullptr, nullptr}, buf_free[2] = {nullptr, nullptr};
     void *d_stage = nullptr;  // host-double staging for uploads
     size_t stage_cap = 0;
     double *d_tab = nullptr;  // [3][Ng] complex phase table, [Ng] winv, [3][Ng] offset-1/2 phase,
@@ -421,6 +427,12 @@ extern "C" void fft_free(fft_t *self) {
             cudaFree(g->d_f);
             cudaFree(g->d_aux);
             cudaFree(g->d_pos);
+            for (int b = 0; b < 2; ++b) {
+                cudaFree(g->d_batch[b]);
+                if (g->up_done[b]) cudaEventDestroy(g->up_done[b]);
+                if (g->buf_free[b]) cudaEventDestroy(g->buf_free[b]);
+            }
+            if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
             cudaFree(g->d_stage);
             cudaFree(g->d_tab);
             fft_plan_destroy(&g->fft);
@@ -917,10 +929,15 @@ extern "C" int fftgal_stage_times(fft_t *grid, double out[FFTGAL_NSTAGES]) {
     return OK;
 }
 
-extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np, double V,
-                                int where, const double los_in[3], double dK, int Nmu, double *K, long *N,
-                                double *Plout, double *Kmu, long *Nmu_count, double *Pmuout) {
+namespace fg {
+// the fused FP32 pipeline of fftgal_power_f32 / fftgal_power_rsd_f32; vel
+// (nullable) displaces every particle along the line of sight while painting
+static int power_f32_run(fft_t *grid, const float *x, const float *y, const float *z, const float *const *vel,
+                         double aH, long Np, double V, int where, const double los_in[3], double dK, int Nmu,
+                         double *K, long *N, double *Plout, double *Kmu, long *Nmu_count, double *Pmuout) {
     if (!grid || !x || !y || !z || Np <= 0 || !(V > 0)) return set_error(ERR_ARG, "fftgal_power_f32: bad arguments");
+    if (vel && (!vel[0] || !vel[1] || !vel[2] || !(aH != 0)))
+        return set_error(ERR_ARG, "fftgal_power_rsd_f32: bad velocities or aH");
     Grid *g = G(grid);
     if (g->prec != 4) return set_error(ERR_STATE, "fftgal_power_f32 needs an FP32 grid");
     FG_TRY(ensure_aux(g));
@@ -930,8 +947,10 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     cudaEvent_t *ev = g->ev;
     if (tm) FG_CUDA(cudaEventRecord(ev[0], st));
     const float *px = x, *py = y, *pz = z;
+    const float *pv[3] = {vel ? vel[0] : nullptr, vel ? vel[1] : nullptr, vel ? vel[2] : nullptr};
     if (where == FFTGAL_MEM_HOST) {
-        const size_t need = (size_t)3 * Np * sizeof(float);
+        const int narr = vel ? 6 : 3;
+        const size_t need = (size_t)narr * Np * sizeof(float);
         if (need > g->pos_cap) {
             cudaFree(g->d_pos);
             g->d_pos = nullptr;
@@ -939,14 +958,26 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
             g->pos_cap = need;
         }
         float *d = (float *)g->d_pos;
-        FG_CUDA(cudaMemcpyAsync(d, x, sizeof(float) * Np, cudaMemcpyHostToDevice, st));
-        FG_CUDA(cudaMemcpyAsync(d + Np, y, sizeof(float) * Np, cudaMemcpyHostToDevice, st));
-        FG_CUDA(cudaMemcpyAsync(d + 2 * Np, z, sizeof(float) * Np, cudaMemcpyHostToDevice, st));
+        const float *src[6] = {x, y, z, pv[0], pv[1], pv[2]};
+        for (int a = 0; a < narr; ++a)
+            FG_CUDA(cudaMemcpyAsync(d + a * Np, src[a], sizeof(float) * Np, cudaMemcpyHostToDevice, st));
         px = d;
         py = d + Np;
         pz = d + 2 * Np;
+        if (vel)
+            for (int a = 0; a < 3; ++a) pv[a] = d + (3 + a) * Np;
     }
     if (tm) FG_CUDA(cudaEventRecord(ev[1], st));
+    double los[3] = {los_in[0], los_in[1], los_in[2]};
+    hat(los);
+    PaintRsd rsd;
+    if (vel) {
+        for (int a = 0; a < 3; ++a) {
+            rsd.v[a] = pv[a];
+            rsd.los[a] = los[a];
+        }
+        rsd.aHinv = 1 / aH;
+    }
     const int Ng = grid->Ng;
     const double Hinv = Ng / grid->L;
     const double H3 = H3_of(g);
@@ -960,7 +991,8 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
         spec[1].offset[a] = remainder(0.5, Ng);
     }
     spec[0].scale = spec[1].scale = Npcinv;
-    FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, 2, st, tm ? ev + 2 : nullptr));
+    FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, 2, st, tm ? ev + 2 : nullptr,
+                 vel ? &rsd : nullptr));
     void *grids[2] = {g->d_f, g->d_aux};
     FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
@@ -970,8 +1002,6 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
     for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
     ++g->version;
-    double los[3] = {los_in[0], los_in[1], los_in[2]};
-    hat(los);
     BinGeometry *geo = nullptr;
     std::vector<double> Psum, Pw;
     const double Vinv = 1 / V;
@@ -1000,6 +1030,85 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     FG_TRY(finish_pmu(geo, Pw, Kmu, Nmu_count, Pmuout));
     if (g->view == FFTGAL_VIEW_SYNC) FG_TRY(device_to_host(g, grid->f, g->pinned));
     return OK;
+}
+}  // namespace fg
+
+extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np, double V,
+                                int where, const double los[3], double dK, int Nmu, double *K, long *N, double *Pl,
+                                double *Kmu, long *Nmu_count, double *Pmu) {
+    return power_f32_run(grid, x, y, z, nullptr, 0, Np, V, where, los, dK, Nmu, K, N, Pl, Kmu, Nmu_count, Pmu);
+}
+
+extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const float *const *y,
+                                      const float *const *z, const long *Np, const double *V,
+                                      const double los[3], double dK, int Nmu, double *K, long *N, double *Pl,
+                                      double *Kmu, long *Nmu_count, double *Pmu) {
+    if (!grid || ncat < 0 || (ncat > 0 && (!x || !y || !z || !Np || !V)))
+        return set_error(ERR_ARG, "fftgal_power_batch_f32: bad arguments");
+    Grid *g = G(grid);
+    if (g->prec != 4) return set_error(ERR_STATE, "fftgal_power_batch_f32 needs an FP32 grid");
+    long maxNp = 0;
+    for (int c = 0; c < ncat; ++c) {
+        if (!x[c] || !y[c] || !z[c] || Np[c] <= 0 || !(V[c] > 0))
+            return set_error(ERR_ARG, "fftgal_power_batch_f32: bad catalog %d", c);
+        maxNp = Np[c] > maxNp ? Np[c] : maxNp;
+    }
+    if (ncat == 0) return OK;
+    if (!g->copy_stream) FG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        if (!g->up_done[b]) FG_CUDA(cudaEventCreateWithFlags(&g->up_done[b], cudaEventDisableTiming));
+        if (!g->buf_free[b]) FG_CUDA(cudaEventCreateWithFlags(&g->buf_free[b], cudaEventDisableTiming));
+    }
+    if ((size_t)3 * maxNp > g->batch_cap) {
+        FG_CUDA(cudaStreamSynchronize(g->stream));
+        FG_CUDA(cudaStreamSynchronize(g->copy_stream));
+        for (int b = 0; b < 2; ++b) {
+            cudaFree(g->d_batch[b]);
+            g->d_batch[b] = nullptr;
+        }
+        g->batch_cap = 0;
+        for (int b = 0; b < 2; ++b) FG_CUDA(cudaMalloc(&g->d_batch[b], sizeof(float) * 3 * maxNp));
+        g->batch_cap = (size_t)3 * maxNp;
+    }
+    const int NK = fftgal_nk(grid->Ng, grid->L, dK);
+    if (NK < 1) return set_error(ERR_ARG, "fftgal_power_batch_f32: bad dK");
+    // catalog c goes to buffer c % 2: its upload waits until the paint of
+    // catalog c - 2 (the buffer's previous user) has read it
+    auto upload = [&](int c) -> int {
+        const int b = c & 1;
+        float *d = g->d_batch[b];
+        FG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->buf_free[b], 0));
+        const float *src[3] = {x[c], y[c], z[c]};
+        for (int a = 0; a < 3; ++a)
+            FG_CUDA(cudaMemcpyAsync(d + (size_t)a * Np[c], src[a], sizeof(float) * Np[c], cudaMemcpyHostToDevice,
+                                    g->copy_stream));
+        FG_CUDA(cudaEventRecord(g->up_done[b], g->copy_stream));
+        return OK;
+    };
+    for (int b = 0; b < 2; ++b) FG_CUDA(cudaEventRecord(g->buf_free[b], g->stream));
+    FG_TRY(upload(0));
+    for (int c = 0; c < ncat; ++c) {
+        const int b = c & 1;
+        if (c + 1 < ncat) FG_TRY(upload(c + 1));
+        FG_CUDA(cudaStreamWaitEvent(g->stream, g->up_done[b], 0));
+        const float *d = g->d_batch[b];
+        const size_t o1 = (size_t)NK * c, o4 = (size_t)NK * 4 * c, om = (size_t)NK * Nmu * c;
+        FG_TRY(power_f32_run(grid, d, d + Np[c], d + 2 * Np[c], nullptr, 0, Np[c], V[c], FFTGAL_MEM_DEVICE, los,
+                             dK, Nmu, K ? K + o1 : nullptr, N ? N + o1 : nullptr, Pl ? Pl + o4 : nullptr,
+                             Kmu ? Kmu + om : nullptr, Nmu_count ? Nmu_count + om : nullptr,
+                             Pmu ? Pmu + om : nullptr));
+        FG_CUDA(cudaEventRecord(g->buf_free[b], g->stream));
+    }
+    FG_CUDA(cudaStreamSynchronize(g->copy_stream));
+    return OK;
+}
+
+extern "C" int fftgal_power_rsd_f32(fft_t *grid, const float *x, const float *y, const float *z, const float *vx,
+                                    const float *vy, const float *vz, long Np, double V, int where,
+                                    const double los[3], double aH, double dK, int Nmu, double *K, long *N,
+                                    double *Pl, double *Kmu, long *Nmu_count, double *Pmu) {
+    const float *vel[3] = {vx, vy, vz};
+    return power_f32_run(grid, x, y, z, vel, aH, Np, V, where, los, dK, Nmu, K, N, Pl, Kmu, Nmu_count, Pmu);
 }
 
 extern "C" int fftgal_g2p_sum(fft_t *grid, const gal_t *pos, double *out) {

@@ -123,6 +123,14 @@ int paint_tiling_create(PaintTiling *t, int Ng);
 void paint_tiling_destroy(PaintTiling *t);
 void paint_scratch_free(PaintScratch *s);
 
+// Redshift-space displacement applied while painting (FP32 positions only):
+// x + (v . los) / aH * los per particle, as src/gal.c:63-77 (gal_rsd) forms it.
+struct PaintRsd {
+    const float *v[3] = {nullptr, nullptr, nullptr};  // device velocities, or null: no displacement
+    double los[3] = {0, 0, 0};                         // already normalised with hat()
+    double aHinv = 0;
+};
+
 // Paint one catalog onto 1 or 2 grids (same tiling, offsets within 1 cell of
 // each other).  pos_prec: 4 (float x,y,z) or 8 (double x,y,z); device pointers.
 // `ev` (optional, 4 events) is recorded after the key, scan, scatter and
@@ -130,7 +138,7 @@ void paint_scratch_free(PaintScratch *s);
 int paint(const PaintTiling *t, PaintScratch *s, int grid_prec,
           const void *x, const void *y, const void *z, int pos_prec, long Np,
           double Hinv, const PaintGridSpec *grids, int ngrids, cudaStream_t st,
-          cudaEvent_t *ev = nullptr);
+          cudaEvent_t *ev = nullptr, const PaintRsd *rsd = nullptr);
 
 // ---- spectral elementwise ----------------------------------------------------
 int scale_grid(void *f, long n, int prec, double s, cudaStream_t st);

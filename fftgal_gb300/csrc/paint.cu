@@ -82,12 +82,27 @@ struct AxisParams {
 
 struct PaintParams {
     AxisParams ax[3];
+    // FP32 redshift-space displacement (v[0] null: none)
+    const float *v[3];
+    float los[3], aHinv;
     int Ng, Ng_pad, ngrids;
     int fb;                  // FP32 path: fraction bits of the packed cell coordinate
     int nt[3];
     const int *tile_of[3];   // [Ng] per axis
     const int *start[3];     // [nt + 1] per axis
 };
+
+// ---- redshift-space displacement ---------------------------------------------
+// x + ((los . v) / aH) los, the operation order of src/gal.c:69-72 in FP32 with
+// explicit FMAs, so the key and scatter kernels displace a particle identically
+__device__ __forceinline__ void rsd_displace(const PaintParams &pp, long p, float pos[3]) {
+    if (!pp.v[0]) return;
+    const float vd = fmaf(pp.los[2], pp.v[2][p], fmaf(pp.los[1], pp.v[1][p], pp.los[0] * pp.v[0][p]));
+    const float s = pp.aHinv * vd;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) pos[a] = fmaf(s, pp.los[a], pos[a]);
+}
+__device__ __forceinline__ void rsd_displace(const PaintParams &, long, double *) {}
 
 // ---- per-axis cell coordinate ----------------------------------------------
 
@@ -222,7 +237,8 @@ __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ 
                                  uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                                  uint32_t *__restrict__ hist) {
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
-        const P pos[3] = {x[p], y[p], z[p]};
+        P pos[3] = {x[p], y[p], z[p]};
+        rsd_displace(pp, p, pos);
         const uint32_t k = paint_key_of<P>(pos, pp);
         key[p] = k;
         rank[p] = atomicAdd(&hist[k], 1u);
@@ -330,7 +346,8 @@ __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restric
         const uint32_t dst = off[key[p]] + rank[p];
         typename Rec<P>::type r;
         if constexpr (sizeof(P) == 4) {
-            const float pos[3] = {x[p], y[p], z[p]};
+            float pos[3] = {x[p], y[p], z[p]};
+            rsd_displace(pp, p, pos);
             uint32_t w[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -990,8 +1007,9 @@ static void split(double v, float &hi, float &lo) {
 
 int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, const void *y, const void *z,
           int pos_prec, long Np, double Hinv, const PaintGridSpec *grids, int ngrids, cudaStream_t st,
-          cudaEvent_t *ev) {
+          cudaEvent_t *ev, const PaintRsd *rsd) {
     if (ngrids < 1 || ngrids > kMaxPaintGrids) return set_error(ERR_ARG, "paint: 1 or 2 grids");
+    if (rsd && rsd->v[0] && pos_prec != 4) return set_error(ERR_ARG, "paint: displacement needs FP32 positions");
     if (pos_prec != grid_prec) return set_error(ERR_ARG, "paint: position precision must match grid precision");
     if (Np < 0 || Np >= (1L << 32)) return set_error(ERR_ARG, "paint: Np out of range");
     for (int g = 1; g < ngrids; ++g)
@@ -1004,6 +1022,13 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     pp.Ng = Ng;
     pp.Ng_pad = 2 * (Ng / 2 + 1);
     pp.ngrids = ngrids;
+    if (rsd && rsd->v[0]) {
+        for (int a = 0; a < 3; ++a) {
+            pp.v[a] = rsd->v[a];
+            pp.los[a] = (float)rsd->los[a];
+        }
+        pp.aHinv = (float)rsd->aHinv;
+    }
     int bits_b = 1;
     while ((1 << bits_b) < Ng) ++bits_b;
     pp.fb = 32 - bits_b < 24 ? 32 - bits_b : 24;  // 2^-24 cell: below FP32 resolution

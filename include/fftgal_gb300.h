@@ -82,6 +82,32 @@ int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z
                      double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
                      double *Pmu);
 
+/* fftgal_power_f32 over a list of ncat catalogs with FP32 positions in host
+ * memory (x[c], y[c], z[c], Np[c] particles, volume V[c]): while catalog c is
+ * painted and transformed, catalog c + 1 is copied to the GPU on a second
+ * stream, so with page-locked host arrays the host-to-device copies hide
+ * behind the computation.  Outputs are the fftgal_power_f32 outputs of each
+ * catalog one after another: K[ncat*NK], N[ncat*NK], Pl[ncat*NK*4],
+ * Kmu/Nmu_count/Pmu[ncat*NK*Nmu] (any may be NULL).  Holds two device buffers
+ * of 3 * max(Np) floats until fft_free. */
+int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const float *const *y,
+                           const float *const *z, const long *Np, const double *V,
+                           const double los[3], double dK, int Nmu, double *K, long *N,
+                           double *Pl, double *Kmu, long *Nmu_count, double *Pmu);
+
+/* fftgal_power_f32 of the redshift-space catalog: every particle is
+ * displaced along the line of sight while it is painted, x + (v . los) / aH
+ * los, as gal_rsd forms it (src/gal.c:63-77), so the P.c sequence
+ * gal_rsd -> fft_p2k -> P -> Pl -> Pmu (src/app/P.c:50-66) is one call with no
+ * displaced copy of the catalog.  vx, vy, vz: FP32 velocities in the same
+ * memory as x, y, z (`where`); los (normalised internally) is both the
+ * displacement direction and the multipole axis. */
+int fftgal_power_rsd_f32(fft_t *grid, const float *x, const float *y, const float *z,
+                         const float *vx, const float *vy, const float *vz, long Np, double V,
+                         int where, const double los[3], double aH, double dK, int Nmu,
+                         double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
+                         double *Pmu);
+
 /* Per-stage device times (ms) of the last fftgal_power_f32 call, measured with
  * CUDA events on the grid's stream: [0] position upload, [1] paint key +
  * histogram, [2] histogram scan, [3] scatter, [4] tile paint, [5] FFT k pass,

@@ -4,6 +4,9 @@ P.c paints on a box of L/fold and lets the cell index wrap, src/app/P.c:35-66),
 Nmu = 10 wedges.  Strong clustering drives the paint's per-block fixed-point
 bound below its maximum, which uniform catalogs never reach.
 
+The redshift-space displacement is applied either by the oracle's gal_rsd
+before painting or, through fftgal_power_rsd_f32, inside the paint itself.
+
 Tolerances: mode counts bit-exact; mean K 1e-12; P_0,2,4 and every wedge within
 1e-4 of (|P_0(k)| + Pshot) for k < 0.8 k_Nyq, every bin within 1e-3.
 """
@@ -23,14 +26,23 @@ def fg():
     return fftgal_gb300
 
 
+def _f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
 @pytest.fixture(scope="module")
-def catalog(oracle_lib):
+def real_space():
     L = 1000.0
-    x, y, z, vx, vy, vz = lognormal_catalog(7, 128, L, 1e6)
+    return L, [_f32(a) for a in lognormal_catalog(7, 128, L, 1e6)]
+
+
+@pytest.fixture(scope="module")
+def catalog(oracle_lib, real_space):
+    L, (x, y, z, vx, vy, vz) = real_space
     # redshift space along z through the oracle's gal_rsd (aH = 1)
     xs, ys, zs = oracle_lib.Oracle.rsd(x, y, z, vx, vy, vz, (0.0, 0.0, 1.0), 1.0)
     # both sides see the same FP32 positions
-    return L, [np.asarray(a, dtype=np.float32).astype(np.float64) for a in (xs, ys, zs)]
+    return L, [_f32(a) for a in (xs, ys, zs)]
 
 
 def _check(got, want, Pshot, kmax):
@@ -59,4 +71,20 @@ def test_lognormal_rsd_folded(fg, oracle_lib, catalog, fold):
     got = g.power_f32(x, y, z, V, los, dK, Nmu=Nmu)
     want = oracle_lib.power_spectrum(Ng, Lfd, x, y, z, los, dK, Nmu=Nmu, V=V)
     assert want["status"] == (0, 0)
+    _check(got, want, V / len(x), 0.8 * np.pi * Ng / Lfd)
+
+
+@pytest.mark.parametrize("los,aH", [((0.0, 0.0, 1.0), 1.0), ((1.0, 1.0, 0.0), 0.7)])
+def test_rsd_fused_into_paint(fg, oracle_lib, real_space, los, aH):
+    """fftgal_power_rsd_f32 (displacement inside the paint, FP32) against the
+    oracle's gal_rsd (FP64, src/gal.c:63-77) followed by the P.c sequence;
+    the displaced positions differ only by FP32 rounding (~1e-4 of a cell)."""
+    L, (x, y, z, vx, vy, vz) = real_space
+    Ng, fold, Nmu = 128, 2, 10
+    Lfd = L / fold
+    dK, V = 2 * np.pi / Lfd, L ** 3
+    g = fg.Grid(Ng, Lfd, precision="f32", host_view="lazy")
+    got = g.power_rsd_f32(x, y, z, vx, vy, vz, V, los, aH, dK, Nmu=Nmu)
+    xs, ys, zs = oracle_lib.Oracle.rsd(x, y, z, vx, vy, vz, los, aH)
+    want = oracle_lib.power_spectrum(Ng, Lfd, xs, ys, zs, los, dK, Nmu=Nmu, V=V)
     _check(got, want, V / len(x), 0.8 * np.pi * Ng / Lfd)
