@@ -89,6 +89,7 @@ struct PaintParams {
     int fb;                  // FP32 path: fraction bits of the packed cell coordinate
     int nt[3];
     const int *tile_of[3];   // [Ng] per axis
+    int tshift[3];           // log2 of the tile extent when every tile of the axis has it, else -1
     const int *start[3];     // [nt + 1] per axis
 };
 
@@ -208,9 +209,16 @@ __device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintPara
             P d;
             coord(pos[a], pp.ax[a], 0, Ng, b0, d);
         }
-        const int ta = pp.tile_of[a][b0];
-        const int t0 = pp.start[a][ta];
-        const int te = pp.start[a][ta + 1] - t0;
+        int ta, t0, te;
+        if (pp.tshift[a] >= 0) {
+            ta = b0 >> pp.tshift[a];
+            t0 = ta << pp.tshift[a];
+            te = 1 << pp.tshift[a];
+        } else {
+            ta = pp.tile_of[a][b0];
+            t0 = pp.start[a][ta];
+            te = pp.start[a][ta + 1] - t0;
+        }
         int rmin = b0 - t0, rmax = b0 - t0;
         for (int g = 1; g < pp.ngrids; ++g) {
             int bg;
@@ -221,7 +229,9 @@ __device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintPara
                 P dg;
                 coord(pos[a], pp.ax[a], g, Ng, bg, dg);
             }
-            const int dl = ((bg - b0 + Ng + 1) % Ng) - 1;  // -1, 0 or +1
+            int dl = bg - b0;  // -1, 0 or +1 after undoing a wrap
+            dl -= dl > 1 ? Ng : 0;
+            dl += dl < -1 ? Ng : 0;
             rmin = min(rmin, b0 - t0 + dl);
             rmax = max(rmax, b0 - t0 + dl);
         }
@@ -1036,6 +1046,13 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     for (int a = 0; a < 3; ++a) {
         pp.nt[a] = t->nt[a];
         pp.tile_of[a] = t->d_tables + t->tab_off[a];
+        {
+            const int ext = Ng / t->nt[a];
+            pp.tshift[a] = -1;
+            if (ext * t->nt[a] == Ng && (ext & (ext - 1)) == 0)
+                for (int b = 0; (1 << b) <= ext; ++b)
+                    if ((1 << b) == ext) pp.tshift[a] = b;
+        }
         pp.start[a] = t->d_tables + t->tab_off[a] + Ng;
         split(Hinv, pp.ax[a].h_hi, pp.ax[a].h_lo);
         pp.ax[a].h = Hinv;
