@@ -238,8 +238,11 @@ int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, l
     FG_TRY(ensure_w32());
     int N1, N2;
     if (!split2(N, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_cols: N=%d", N);
-    // C columns per CTA: threads = C*N2 around 256, C >= 8 for 64-byte rows
-    int logC = 3;
+    // C columns per CTA: threads = C*N2 around 256, C >= 8 for 64-byte rows;
+    // along a widely strided axis (the i pass) C = 16, so every row access
+    // is a 128-byte run (measured 15 % faster at Ng = 1024; the j pass is
+    // faster with C = 8 and two CTAs per SM)
+    int logC = es * (long)sizeof(float2) > (1L << 20) ? 4 : 3;
     while ((1 << logC) * N2 < 256 && logC < 5) ++logC;
     while ((1 << logC) * N2 > 512 && logC > 0) --logC;
     const int C = 1 << logC;
@@ -279,8 +282,8 @@ int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int n
     if (!split2(M, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_k_r2c: Ng=%d", Ng);
     const int Ng_pad = 2 * (M + 1);
     const long nrows = (long)Ng * Ng;
-    int R = 1;
-    while (R * N2 < 256 && R < 64) R *= 2;
+    int R = 1;  // rows per CTA: threads = R*N2 around 64 (small CTAs, many per SM)
+    while (R * N2 < 64 && R < 64) R *= 2;
     const int threads = R * N2;
     const int P = N2 * (N1 + 1), P2 = M + 1;
     const size_t smem = (size_t)R * (P > P2 ? P : P2) * sizeof(float2);
