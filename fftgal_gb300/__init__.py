@@ -92,6 +92,8 @@ SIGNATURES = {
     "fftgal_nk": (C.c_int, [C.c_int, C.c_double, C.c_double]),
     "fftgal_power_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                    C.c_int, _dp, C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
+    "fftgal_window_box": (C.c_int, [_P_F, C.c_int]),
+    "fftgal_window_sphere": (C.c_int, [_P_F, C.c_int]),
     "fftgal_power_batch_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp, _dp,
                                          C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_power_rsd_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -302,6 +304,14 @@ class Grid:
         out = np.zeros(NSTAGES)
         _check(lib().fftgal_stage_times(self.p, out.ctypes.data_as(_dp)))
         return dict(zip(STAGES, out.tolist()))
+
+    def window_box(self, Ngsub: int):
+        """Sub-box window deconvolution of the real-space grid (src/app/Psb.c:76-83)."""
+        _check(lib().fftgal_window_box(self.p, int(Ngsub)))
+
+    def window_sphere(self, Ngsub: int):
+        """Sub-sphere window deconvolution of the real-space grid (src/app/Pss.c:72-84)."""
+        _check(lib().fftgal_window_sphere(self.p, int(Ngsub)))
 
     def copy_from(self, ptr: int):
         """Fill the canonical grid from a CUDA-visible buffer (raw pointer)."""

@@ -1039,6 +1039,22 @@ extern "C" int fftgal_power_f32(fft_t *grid, const float *x, const float *y, con
     return power_f32_run(grid, x, y, z, nullptr, 0, Np, V, where, los, dK, Nmu, K, N, Pl, Kmu, Nmu_count, Pmu);
 }
 
+extern "C" int fftgal_window_box(fft_t *grid, int Ngsub) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    FG_TRY(enter(grid, true));
+    FG_TRY(window_box(g->d_f, grid->Ng, g->prec, Ngsub, g->stream));
+    return leave(grid, true);
+}
+
+extern "C" int fftgal_window_sphere(fft_t *grid, int Ngsub) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    FG_TRY(enter(grid, true));
+    FG_TRY(window_sphere(g->d_f, grid->Ng, g->prec, Ngsub, g->stream));
+    return leave(grid, true);
+}
+
 extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const float *const *y,
                                       const float *const *z, const long *Np, const double *V,
                                       const double los[3], double dK, int Nmu, double *K, long *N, double *Pl,

@@ -153,6 +153,9 @@ int interlace_average(void *f, const void *fdual, long n, int prec, cudaStream_t
 int interlace_finish(void *A, const void *B, int Ng, int prec, double H3, const void *d_tab,
                      const void *d_winv, cudaStream_t st);
 int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStream_t st);
+// real-space sub-volume window deconvolutions of src/app/Psb.c:76-83 and Pss.c:72-84
+int window_box(void *f, int Ng, int prec, int Ngsub, cudaStream_t st);
+int window_sphere(void *f, int Ng, int prec, int Ngsub, cudaStream_t st);
 int convert_grid(void *dst, int dst_prec, const void *src, int src_prec, long n, cudaStream_t st);
 
 // ---- binning -----------------------------------------------------------------

@@ -311,6 +311,108 @@ int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStre
     return OK;
 }
 
+// ---- sub-volume window deconvolution of the real-space grid ----------------------------------
+// Sub-box (src/app/Psb.c:76-83): cells (i, j, k) in (-Ngsub, Ngsub)^3, wrapped
+// mod Ng (distinct cells for Ngsub <= Ng/2), times Ngsub^3 / ((Ngsub-|i|)
+// (Ngsub-|j|)(Ngsub-|k|)); one thread per (i, j, k).  FP64 grids evaluate the
+// factor in the reference's order; FP32 grids as a product of per-axis factors.
+template <typename T>
+__global__ void window_box_kernel(T *f, int Ng, int Ng_pad, int Ngsub) {
+    const long n1 = 2L * Ngsub - 1, n = n1 * n1 * n1;
+    const double Ngsub3 = (double)Ngsub * Ngsub * Ngsub;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(e / (n1 * n1)) - (Ngsub - 1);
+        const int j = (int)((e / n1) % n1) - (Ngsub - 1);
+        const int k = (int)(e % n1) - (Ngsub - 1);
+        T &v = f[((long)((i + Ng) % Ng) * Ng + (j + Ng) % Ng) * Ng_pad + (k + Ng) % Ng];
+        if constexpr (sizeof(T) == 8) {
+            const double Winv = __ddiv_rn(Ngsub3, __dmul_rn(__dmul_rn((double)(Ngsub - abs(i)), (double)(Ngsub - abs(j))),
+                                                          (double)(Ngsub - abs(k))));
+            v = __dmul_rn(v, Winv);
+        } else {
+            const float s = (float)Ngsub;
+            v *= (s / (float)(Ngsub - abs(i))) * (s / (float)(Ngsub - abs(j))) * (s / (float)(Ngsub - abs(k)));
+        }
+    }
+}
+
+// Sub-sphere (src/app/Pss.c:72-84): index range (-Ngbnd, Ngbnd)^3 with Ngbnd =
+// ceil(sqrt(3) Ngsub) > Ng/2, so some cells are reached by two images per
+// axis and multiplied once per image with d2 < 0.99 D2.  One thread per cell
+// applies its images in the reference's loop order (i, then j, then k
+// ascending); d2_max is the largest integer d2 below 0.99 D2.
+template <typename T>
+__global__ void window_sphere_kernel(T *f, int Ng, int Ng_pad, int Ngbnd, double D2, long d2_max) {
+    const long n = (long)Ng * Ng * Ng;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const int c[3] = {(int)(e / ((long)Ng * Ng)), (int)((e / Ng) % Ng), (int)(e % Ng)};
+        int img[3][2], nimg[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {  // images c - Ng, c (ascending) inside the range
+            nimg[a] = 0;
+            if (c[a] - Ng > -Ngbnd) img[a][nimg[a]++] = c[a] - Ng;
+            if (c[a] < Ngbnd) img[a][nimg[a]++] = c[a];
+        }
+        if (!nimg[0] || !nimg[1] || !nimg[2]) continue;
+        T &v = f[((long)c[0] * Ng + c[1]) * Ng_pad + c[2]];
+        T x = v;
+        for (int p = 0; p < nimg[0]; ++p)
+            for (int q = 0; q < nimg[1]; ++q)
+                for (int r = 0; r < nimg[2]; ++r) {
+                    const long i = img[0][p], j = img[1][q], k = img[2][r];
+                    const long d2i = i * i + j * j + k * k;
+                    if (d2i > d2_max) continue;
+                    if constexpr (sizeof(T) == 8) {
+                        const double d2 = __dadd_rn(__dadd_rn((double)(i * i), (double)(j * j)), (double)(k * k));
+                        const double dD = __dsqrt_rn(__ddiv_rn(d2, D2));
+                        const double u = __dsub_rn(1.0, dD);
+                        const double Winv =
+                            __ddiv_rn(1.0, __dmul_rn(__dmul_rn(u, u), __dadd_rn(1.0, __dmul_rn(0.5, dD))));
+                        x = __dmul_rn(x, Winv);
+                    } else {
+                        // 1 - dD = (D2 - d2) / (D2 (1 + dD)), free of the cancellation
+                        // near the sphere's edge (D2 - d2 is an exact integer)
+                        const float fD2 = (float)D2;
+                        const float dD = sqrtf((float)d2i / fD2);
+                        const float u = (float)((long)D2 - d2i) / (fD2 * (1.f + dD));
+                        x *= 1.f / (u * u * (1.f + 0.5f * dD));
+                    }
+                }
+        v = x;
+    }
+}
+
+int window_box(void *f, int Ng, int prec, int Ngsub, cudaStream_t st) {
+    if (Ngsub < 1 || 2 * Ngsub > Ng) return set_error(ERR_ARG, "window_box: need 1 <= Ngsub <= Ng/2");
+    const long n1 = 2L * Ngsub - 1;
+    const int Ng_pad = 2 * (Ng / 2 + 1);
+    if (prec == 4)
+        window_box_kernel<float><<<grid_blocks(n1 * n1 * n1, 256), 256, 0, st>>>((float *)f, Ng, Ng_pad, Ngsub);
+    else
+        window_box_kernel<double><<<grid_blocks(n1 * n1 * n1, 256), 256, 0, st>>>((double *)f, Ng, Ng_pad, Ngsub);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+int window_sphere(void *f, int Ng, int prec, int Ngsub, cudaStream_t st) {
+    if (Ngsub < 1 || 2 * Ngsub > Ng) return set_error(ERR_ARG, "window_sphere: need 1 <= Ngsub <= Ng/2");
+    volatile double D2 = 3.0 * Ngsub * Ngsub;
+    const int Ngbnd = (int)ceil(sqrt((double)D2));
+    if (Ngbnd >= Ng) return set_error(ERR_ARG, "window_sphere: Ngsub too large for Ng");
+    volatile double lim = 0.99 * D2;
+    long d2_max = (long)floor((double)lim);
+    while (d2_max >= 0 && !((double)d2_max < (double)lim)) --d2_max;  // largest integer d2 < 0.99 D2
+    const int Ng_pad = 2 * (Ng / 2 + 1);
+    const long n = (long)Ng * Ng * Ng;
+    if (prec == 4)
+        window_sphere_kernel<float><<<grid_blocks(n, 256), 256, 0, st>>>((float *)f, Ng, Ng_pad, Ngbnd, D2, d2_max);
+    else
+        window_sphere_kernel<double><<<grid_blocks(n, 256), 256, 0, st>>>((double *)f, Ng, Ng_pad, Ngbnd, D2,
+                                                                          d2_max);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
 // ---- precision conversion (device grid <-> pinned host view) ---------------------------------
 template <typename D, typename S>
 __global__ void convert_kernel(D *d, const S *__restrict__ s, long n) {

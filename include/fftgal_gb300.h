@@ -82,6 +82,18 @@ int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z
                      double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
                      double *Pmu);
 
+/* Sub-volume window deconvolution of the real-space grid on the GPU, the
+ * host loops of src/app/Psb.c:76-83 (sub-box: cells (i,j,k) in (-Ngsub,
+ * Ngsub)^3 wrapped mod Ng, times Ngsub^3 / ((Ngsub-|i|)(Ngsub-|j|)(Ngsub-|k|)))
+ * and src/app/Pss.c:72-84 (sub-sphere: d2 < 0.99 * 3 Ngsub^2 over
+ * (-ceil(sqrt(3) Ngsub), ceil(sqrt(3) Ngsub))^3 wrapped mod Ng, times
+ * 1 / ((1 - dD)^2 (1 + dD/2)), a cell reached by several wrapped indices
+ * multiplied once per index, as the loop does).  Call after fft_k2x, in
+ * place of the loop over grid->f; FP64 grids reproduce the loop bit for bit.
+ * 1 <= Ngsub <= Ng/2. */
+int fftgal_window_box(fft_t *grid, int Ngsub);
+int fftgal_window_sphere(fft_t *grid, int Ngsub);
+
 /* fftgal_power_f32 over a list of ncat catalogs with FP32 positions in host
  * memory (x[c], y[c], z[c], Np[c] particles, volume V[c]): while catalog c is
  * painted and transformed, catalog c + 1 is copied to the GPU on a second

@@ -97,6 +97,8 @@ class Oracle:
             lib.og_rsd.argtypes = [C.c_long, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                    C.c_double, _dp, _dp, _dp]
             lib.og_wrap.argtypes = [C.c_long, _dp, _dp, _dp, C.c_double]
+            lib.og_window_box.argtypes = [C.c_void_p, C.c_int]
+            lib.og_window_sphere.argtypes = [C.c_void_p, C.c_int]
             cls._lib = lib
         return cls._lib
 
@@ -172,6 +174,14 @@ class Oracle:
         out = np.zeros(len(x))
         self.lib().og_g2p(self._g, len(x), _ptr(x), _ptr(y), _ptr(z), _ptr(out))
         return out
+
+    def window_box(self, Ngsub: int):
+        """src/app/Psb.c:76-83 on the real-space grid."""
+        self.lib().og_window_box(self._g, int(Ngsub))
+
+    def window_sphere(self, Ngsub: int):
+        """src/app/Pss.c:72-84 on the real-space grid."""
+        self.lib().og_window_sphere(self._g, int(Ngsub))
 
     def power(self, Np: int, V: float, Nr: int = 0):
         self.lib().og_power(self._g, int(Np), float(V), int(Nr))

@@ -407,3 +407,38 @@ void og_rsd(long Np, const double *x, const double *y, const double *z,
         zo[p] = z[p] + aHinv * vdl * los[2];
     }
 }
+
+/* sub-box window deconvolution of the real-space grid, the host loop of
+ * src/app/Psb.c:76-83 (also :126-133): cells (i, j, k) in (-Ngsub, Ngsub)^3,
+ * wrapped mod Ng, times Ngsub^3 / ((Ngsub-|i|)(Ngsub-|j|)(Ngsub-|k|)) */
+void og_window_box(og_grid *g, int Ngsub) {
+    const int Ng = g->Ng;
+    double Ngsub3 = (double)Ngsub * Ngsub * Ngsub;
+    for (int i = -Ngsub + 1; i < Ngsub; ++i)
+        for (int j = -Ngsub + 1; j < Ngsub; ++j)
+            for (int k = -Ngsub + 1; k < Ngsub; ++k) {
+                double Winv = Ngsub3 / ((double)(Ngsub - abs(i)) * (Ngsub - abs(j)) * (Ngsub - abs(k)));
+                OF(g, (i + Ng) % Ng, (j + Ng) % Ng, (k + Ng) % Ng) *= Winv;
+            }
+}
+
+/* sub-sphere window deconvolution, the host loop of src/app/Pss.c:72-84:
+ * cells with d2 = i^2 + j^2 + k^2 < 0.99 * 3 Ngsub^2 over (-Ngbnd, Ngbnd)^3,
+ * Ngbnd = ceil(sqrt(3) Ngsub), wrapped mod Ng (an index range wider than
+ * Ng/2 reaches some cells twice, each time multiplying again), times
+ * 1 / ((1 - dD)^2 (1 + dD/2)), dD = sqrt(d2 / D2) */
+void og_window_sphere(og_grid *g, int Ngsub) {
+    const int Ng = g->Ng;
+    double D2 = 3.0 * Ngsub * Ngsub;
+    int Ngbnd = (int)ceil(sqrt(D2));
+    for (int i = -Ngbnd + 1; i < Ngbnd; ++i)
+        for (int j = -Ngbnd + 1; j < Ngbnd; ++j)
+            for (int k = -Ngbnd + 1; k < Ngbnd; ++k) {
+                double d2 = (double)i * i + (double)j * j + (double)k * k;
+                if (d2 < 0.99 * D2) {
+                    double dD = sqrt(d2 / D2);
+                    double Winv = 1 / ((1 - dD) * (1 - dD) * (1 + 0.5 * dD));
+                    OF(g, (i + Ng) % Ng, (j + Ng) % Ng, (k + Ng) % Ng) *= Winv;
+                }
+            }
+}
