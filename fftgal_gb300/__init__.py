@@ -94,6 +94,7 @@ SIGNATURES = {
                                    C.c_int, _dp, C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_window_box": (C.c_int, [_P_F, C.c_int]),
     "fftgal_window_sphere": (C.c_int, [_P_F, C.c_int]),
+    "fftgal_dl_sub": (C.c_int, [_P_F, C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp]),
     "fftgal_power_batch_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp, _dp,
                                          C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_power_rsd_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -312,6 +313,15 @@ class Grid:
     def window_sphere(self, Ngsub: int):
         """Sub-sphere window deconvolution of the real-space grid (src/app/Pss.c:72-84)."""
         _check(lib().fftgal_window_sphere(self.p, int(Ngsub)))
+
+    def dl_sub(self, sphere: int, Nsub: int, los_list, bias: float = 1.0) -> np.ndarray:
+        """Super-sample modes [nlos, 3, Nsub^3] of the k-space field held by the
+        grid (src/app/DLsb.c / DLss.c per line of sight)."""
+        l = np.ascontiguousarray(np.asarray(los_list, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros((len(l), 3, Nsub ** 3))
+        _check(lib().fftgal_dl_sub(self.p, int(sphere), int(Nsub), len(l), l.ctypes.data_as(_dp), float(bias),
+                                   out.ctypes.data_as(_dp)))
+        return out
 
     def copy_from(self, ptr: int):
         """Fill the canonical grid from a CUDA-visible buffer (raw pointer)."""

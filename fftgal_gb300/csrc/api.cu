@@ -1055,6 +1055,66 @@ extern "C" int fftgal_window_sphere(fft_t *grid, int Ngsub) {
     return leave(grid, true);
 }
 
+extern "C" int fftgal_dl_sub(fft_t *grid, int sphere, int Nsub, int nlos, const double *los, double bias,
+                             double *DeltaL) {
+    if (!grid || !los || !DeltaL || nlos < 1 || !(bias != 0)) return set_error(ERR_ARG, "fftgal_dl_sub: bad arguments");
+    Grid *g = G(grid);
+    const int Ng = grid->Ng;
+    if (Nsub < 2 || Ng % Nsub) return set_error(ERR_ARG, "fftgal_dl_sub: Nsub must divide Ng, Nsub >= 2");
+    const int Ngsub = Ng / Nsub, nsub3 = Nsub * Nsub * Nsub;
+    FG_TRY(enter(grid, true));
+    FG_TRY(ensure_aux(g));
+    cudaStream_t st = g->stream;
+    // the unfiltered k-space field, filtered anew for every (line of sight, multipole)
+    FG_CUDA(cudaMemcpyAsync(g->d_aux, g->d_f, (size_t)g->prec * grid->Ng3_pad, cudaMemcpyDeviceToDevice, st));
+    // window tables, evaluated on the host like src/app/DLsb.c:44-50 / DLss.c:18-20,78
+    std::vector<double> tab;
+    if (sphere) {
+        const long h = Ng / 2, n2max = 3 * h * h;
+        tab.assign((size_t)n2max + 1, 0.0);
+        for (long n2 = 1; n2 <= n2max; ++n2) {
+            const double Kamp = sqrt((double)n2);
+            volatile double KR = Kamp * M_PI * 1.73205080756887729352744634151 / Nsub;  // M_SQRT3
+            volatile double KRcos = KR * cos(KR);  // kept separate: no FMA contraction
+            tab[n2] = 3 * (sin(KR) - KRcos) / (KR * KR * KR);
+        }
+    } else {
+        tab.assign((size_t)7 * Ng, 0.0);
+        tab[0] = 1;
+        for (int i = 1; i < Ng; ++i) tab[i] = sin(M_PI * i / Nsub) / sin(M_PI * i / Ng) / Ngsub;
+        for (int i = 0; i < 3 * Ng; ++i) {
+            tab[Ng + 2 * i] = cos(M_PI * i * (Ngsub - 1) / Ng);
+            tab[Ng + 2 * i + 1] = sin(M_PI * i * (Ngsub - 1) / Ng);
+        }
+    }
+    double *d_tab = nullptr, *d_out = nullptr;
+    FG_CUDA(cudaMalloc(&d_tab, sizeof(double) * tab.size()));
+    cudaError_t e = cudaMalloc(&d_out, sizeof(double) * (size_t)nsub3 * 3 * nlos);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, st);
+    int rc = cuda_check(e, "fftgal_dl_sub tables");
+    const double L3 = grid->L * grid->L * grid->L;
+    void *grids[1] = {g->d_f};
+    for (int l = 0; l < nlos && rc == OK; ++l) {
+        double lh[3] = {los[3 * l], los[3 * l + 1], los[3 * l + 2]};
+        hat(lh);
+        for (int iL = 0; iL < 3 && rc == OK; ++iL) {
+            rc = dl_filter(g->d_f, g->d_aux, Ng, g->prec, sphere, d_tab, lh, iL, st);
+            if (rc == OK) rc = fft_c2r(&g->fft, grids, 1, st);
+            if (rc == OK) rc = scale_grid(g->d_f, grid->Ng3_pad, g->prec, 1 / L3, st);
+            if (rc == OK) rc = dl_sample(g->d_f, Ng, g->prec, Nsub, bias, d_out + (size_t)(3 * l + iL) * nsub3, st);
+        }
+    }
+    if (rc == OK)
+        rc = cuda_check(cudaMemcpyAsync(DeltaL, d_out, sizeof(double) * (size_t)nsub3 * 3 * nlos,
+                                        cudaMemcpyDeviceToHost, st), "fftgal_dl_sub results");
+    if (rc == OK) rc = cuda_check(cudaStreamSynchronize(st), "fftgal_dl_sub");
+    cudaFree(d_tab);
+    cudaFree(d_out);
+    FG_TRY(rc);
+    return leave(grid, true);
+}
+
 extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const float *const *y,
                                       const float *const *z, const long *Np, const double *V,
                                       const double los[3], double dK, int Nmu, double *K, long *N, double *Pl,

@@ -156,6 +156,11 @@ int power_inplace(void *f, int Ng, int prec, double Vinv, double Pshot, cudaStre
 // real-space sub-volume window deconvolutions of src/app/Psb.c:76-83 and Pss.c:72-84
 int window_box(void *f, int Ng, int prec, int Ngsub, cudaStream_t st);
 int window_sphere(void *f, int Ng, int prec, int Ngsub, cudaStream_t st);
+// super-sample filters of src/app/DLsb.c:67-85 / DLss.c:65-81 (los normalised) and the
+// corner samples of their c2r output
+int dl_filter(void *dst, const void *src, int Ng, int prec, int sphere, const double *d_tab, const double los[3],
+              int iL, cudaStream_t st);
+int dl_sample(const void *f, int Ng, int prec, int Nsub, double bias, double *d_out, cudaStream_t st);
 int convert_grid(void *dst, int dst_prec, const void *src, int src_prec, long n, cudaStream_t st);
 
 // ---- binning -----------------------------------------------------------------

@@ -382,6 +382,103 @@ __global__ void window_sphere_kernel(T *f, int Ng, int Ng_pad, int Ngbnd, double
     }
 }
 
+// ---- super-sample filters of the k-space field (src/app/DLsb.c:67-85, DLss.c:65-81) -------
+// dst <- L_iL(mu^2) W(k) src over the half spectrum, the k = 0 real part
+// zeroed and its imaginary part kept.  SPHERE: W = top hat of |n| pi sqrt(3) /
+// Nsub, tab[n^2] (host-evaluated); else W = Wamp_i Wamp_j Wamp_k exp(i pi
+// (i+j+k)(Ngsub-1)/Ng) from tab = Wamp[Ng] | (cos, sin)[3 Ng].  FP64 grids in
+// the reference's operation order.
+__device__ __forceinline__ int kval_dl(int i, int Ng) { return 2 * i < Ng ? i : i - Ng; }
+
+template <typename T, bool SPHERE>
+__global__ void dl_filter_kernel(T *dst, const T *__restrict__ src, int Ng, const double *__restrict__ tab,
+                                 double l0, double l1, double l2, int iL) {
+    using T2 = vec2_t<T>;
+    const int nh = Ng / 2 + 1;
+    const T2 *s2 = reinterpret_cast<const T2 *>(src);
+    T2 *d2 = reinterpret_cast<T2 *>(dst);
+    FG_FOR_MODES(Ng, nh) {
+        const T2 fv = s2[e];
+        if (e == 0) {
+            d2[0] = mk2<T2>(0, fv.y);
+            continue;
+        }
+        const int ki = kval_dl(i, Ng), kj = kval_dl(j, Ng), kk = kval_dl(k, Ng);
+        const double n2 = (double)((long)ki * ki + (long)kj * kj + (long)kk * kk);
+        if constexpr (sizeof(T) == 8) {
+            const double Kamp = __dsqrt_rn(n2);
+            const double num = __dadd_rn(__dadd_rn(__dmul_rn((double)ki, l0), __dmul_rn((double)kj, l1)),
+                                         __dmul_rn((double)kk, l2));
+            const double q = __ddiv_rn(num, Kamp);
+            const double mu2 = __dmul_rn(q, q);
+            const double Leg = iL == 0 ? 1.0
+                               : iL == 1 ? __dsub_rn(__dmul_rn(1.5, mu2), 0.5)
+                                         : __dadd_rn(__dmul_rn(__dsub_rn(__dmul_rn(4.375, mu2), 3.75), mu2), 0.375);
+            if constexpr (SPHERE) {
+                const double LW = __dmul_rn(Leg, tab[(long)n2]);
+                d2[e] = mk2<T2>(__dmul_rn(fv.x, LW), __dmul_rn(fv.y, LW));
+            } else {
+                const double Wamp3 = __dmul_rn(__dmul_rn(tab[i], tab[j]), tab[k]);
+                const double *ph = tab + Ng + 2 * (i + j + k);
+                const double Wre = __dmul_rn(ph[0], Wamp3), Wim = __dmul_rn(ph[1], Wamp3);
+                d2[e] = mk2<T2>(__dmul_rn(Leg, __dsub_rn(__dmul_rn(fv.x, Wre), __dmul_rn(fv.y, Wim))),
+                                __dmul_rn(Leg, __dadd_rn(__dmul_rn(fv.x, Wim), __dmul_rn(fv.y, Wre))));
+            }
+        } else {
+            const float q = ((float)ki * (float)l0 + (float)kj * (float)l1 + (float)kk * (float)l2) *
+                            rsqrtf((float)n2);
+            const float mu2 = q * q;
+            const float Leg = iL == 0 ? 1.f : iL == 1 ? 1.5f * mu2 - 0.5f : (4.375f * mu2 - 3.75f) * mu2 + 0.375f;
+            if constexpr (SPHERE) {
+                const float LW = Leg * (float)tab[(long)n2];
+                d2[e] = mk2<T2>(fv.x * LW, fv.y * LW);
+            } else {
+                const float Wamp3 = (float)tab[i] * (float)tab[j] * (float)tab[k];
+                const double *ph = tab + Ng + 2 * (i + j + k);
+                const float Wre = (float)ph[0] * Wamp3, Wim = (float)ph[1] * Wamp3;
+                d2[e] = mk2<T2>(Leg * (fv.x * Wre - fv.y * Wim), Leg * (fv.x * Wim + fv.y * Wre));
+            }
+        }
+    }
+}
+
+int dl_filter(void *dst, const void *src, int Ng, int prec, int sphere, const double *d_tab, const double los[3],
+              int iL, cudaStream_t st) {
+#define FG_DL(T, S)                                                                                              \
+    dl_filter_kernel<T, S><<<chunk_blocks(Ng), 256, 0, st>>>((T *)dst, (const T *)src, Ng, d_tab, los[0], los[1], \
+                                                            los[2], iL)
+    if (prec == 4) {
+        if (sphere) FG_DL(float, true); else FG_DL(float, false);
+    } else {
+        if (sphere) FG_DL(double, true); else FG_DL(double, false);
+    }
+#undef FG_DL
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+// out[s] = F(isub*Ngsub, jsub*Ngsub, ksub*Ngsub) / bias, s = (isub*Nsub + jsub)*Nsub + ksub
+template <typename T>
+__global__ void dl_sample_kernel(const T *__restrict__ f, int Ng, int Nsub, double bias, double *out) {
+    const int n = Nsub * Nsub * Nsub;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int Ngsub = Ng / Nsub, Ng_pad = 2 * (Ng / 2 + 1);
+    const int is = s / (Nsub * Nsub), js = (s / Nsub) % Nsub, ks = s % Nsub;
+    out[s] = __ddiv_rn((double)f[((long)(is * Ngsub) * Ng + js * Ngsub) * Ng_pad + ks * Ngsub], bias);
+}
+
+int dl_sample(const void *f, int Ng, int prec, int Nsub, double bias, double *d_out, cudaStream_t st) {
+    const int n = Nsub * Nsub * Nsub;
+    if (prec == 4)
+        dl_sample_kernel<float><<<(unsigned)ceil_div(n, 128), 128, 0, st>>>((const float *)f, Ng, Nsub, bias, d_out);
+    else
+        dl_sample_kernel<double><<<(unsigned)ceil_div(n, 128), 128, 0, st>>>((const double *)f, Ng, Nsub, bias,
+                                                                            d_out);
+    FG_LAUNCHED(1);
+    return OK;
+}
+
 int window_box(void *f, int Ng, int prec, int Ngsub, cudaStream_t st) {
     if (Ngsub < 1 || 2 * Ngsub > Ng) return set_error(ERR_ARG, "window_box: need 1 <= Ngsub <= Ng/2");
     const long n1 = 2L * Ngsub - 1;

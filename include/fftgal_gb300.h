@@ -94,6 +94,21 @@ int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z
 int fftgal_window_box(fft_t *grid, int Ngsub);
 int fftgal_window_sphere(fft_t *grid, int Ngsub);
 
+/* Super-sample modes of sub-volumes, the per-line-of-sight loop of
+ * src/app/DLsb.c:56-92 (sphere = 0: sub-box window) and src/app/DLss.c:54-90
+ * (sphere = 1: top-hat sphere of radius sqrt(3) L / (2 Nsub)).  On entry the
+ * grid holds the unfiltered k-space field (fft_p2g + fft_x2k(grid, 0), as the
+ * drivers prepare it).  For each of the nlos lines of sight los[3*l..3*l+2]
+ * and each multipole iL = 0, 1, 2 the field is multiplied by L_iL(mu^2) W(k),
+ * transformed to configuration space (fft_k2x without phase) and sampled at
+ * the sub-volume corners: DeltaL[(3*l + iL)*Nsub^3 + (isub*Nsub + jsub)*Nsub +
+ * ksub] = F(isub*Ngsub, jsub*Ngsub, ksub*Ngsub) / bias.  The unfiltered field
+ * stays on the GPU between the 3 * nlos filters (no exportf/importf round
+ * trips); on return the grid holds the last filtered configuration-space
+ * field, as after the drivers' loop.  Nsub >= 2 must divide Ng. */
+int fftgal_dl_sub(fft_t *grid, int sphere, int Nsub, int nlos, const double *los, double bias,
+                  double *DeltaL);
+
 /* fftgal_power_f32 over a list of ncat catalogs with FP32 positions in host
  * memory (x[c], y[c], z[c], Np[c] particles, volume V[c]): while catalog c is
  * painted and transformed, catalog c + 1 is copied to the GPU on a second

@@ -98,6 +98,7 @@ class Oracle:
                                    C.c_double, _dp, _dp, _dp]
             lib.og_wrap.argtypes = [C.c_long, _dp, _dp, _dp, C.c_double]
             lib.og_window_box.argtypes = [C.c_void_p, C.c_int]
+            lib.og_dl.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, C.c_double, _dp]
             lib.og_window_sphere.argtypes = [C.c_void_p, C.c_int]
             cls._lib = lib
         return cls._lib
@@ -182,6 +183,14 @@ class Oracle:
     def window_sphere(self, Ngsub: int):
         """src/app/Pss.c:72-84 on the real-space grid."""
         self.lib().og_window_sphere(self._g, int(Ngsub))
+
+    def dl(self, sphere: int, Nsub: int, los, iL: int, bias: float = 1.0) -> np.ndarray:
+        """One line-of-sight, one-multipole step of src/app/DLsb.c:56-92
+        (sphere=0) / DLss.c:54-90 (sphere=1); the grid must hold the
+        unfiltered k-space field and is left in configuration space."""
+        out = np.zeros(Nsub ** 3)
+        self.lib().og_dl(self._g, int(sphere), int(Nsub), _ptr(_f64(los).copy()), int(iL), float(bias), _ptr(out))
+        return out
 
     def power(self, Np: int, V: float, Nr: int = 0):
         self.lib().og_power(self._g, int(Np), float(V), int(Nr))

@@ -442,3 +442,60 @@ void og_window_sphere(og_grid *g, int Ngsub) {
                 }
             }
 }
+
+/* super-sample modes of sub-volumes, the loop body of src/app/DLsb.c:56-92
+ * (box, sphere = 0) and src/app/DLss.c:54-90 (sphere = 1) for one line of
+ * sight and one multipole iL: the grid holds the unfiltered k-space field on
+ * entry; F(k) <- L_iL(mu^2) W(k) F(k) (the k = 0 real part zeroed), c2r
+ * (fft_k2x without phase), then out[(isub*Nsub + jsub)*Nsub + ksub] =
+ * F(isub*Ngsub, jsub*Ngsub, ksub*Ngsub) / bias.  los is normalised here. */
+static double og_tophat(double KR) { return 3 * (sin(KR) - KR * cos(KR)) / cube(KR); }
+
+void og_dl(og_grid *g, int sphere, int Nsub, const double los_in[3], int iL, double bias, double *out) {
+    const int Ng = g->Ng, Ngsub = Ng / Nsub;
+    double los[3] = {los_in[0], los_in[1], los_in[2]};
+    og_hat(los);
+    double *Wamp = (double *)malloc(sizeof(double) * Ng);
+    double *Wph = (double *)malloc(sizeof(double) * 6 * Ng);
+    double *Kval = (double *)malloc(sizeof(double) * Ng);
+    Wamp[0] = 1;
+    for (int i = 1; i < Ng; ++i) Wamp[i] = sin(M_PI * i / Nsub) / sin(M_PI * i / Ng) / Ngsub;
+    for (int i = 0; i < 3 * Ng; ++i) {
+        Wph[2 * i] = cos(M_PI * i * (Ngsub - 1) / Ng);
+        Wph[2 * i + 1] = sin(M_PI * i * (Ngsub - 1) / Ng);
+    }
+    Kval[0] = 0;
+    for (int i = 1; i <= Ng / 2; ++i) {
+        Kval[i] = i;
+        Kval[Ng - i] = -i;
+    }
+    g->f[0] = 0;
+    for (int i = 0; i < Ng; ++i)
+        for (int j = 0; j < Ng; ++j)
+            for (int k = (i == 0 && j == 0); k <= Ng / 2; ++k) {
+                double Kamp = sqrt(sq(Kval[i]) + sq(Kval[j]) + sq(Kval[k]));
+                double mu2 = sq((Kval[i] * los[0] + Kval[j] * los[1] + Kval[k] * los[2]) / Kamp);
+                double Legendre[3] = {1, 1.5 * mu2 - 0.5, (4.375 * mu2 - 3.75) * mu2 + 0.375};
+                if (sphere) {
+                    double W = og_tophat(Kamp * M_PI * OG_SQRT3 / Nsub);
+                    ORE(g, i, j, k) *= Legendre[iL] * W;
+                    OIM(g, i, j, k) *= Legendre[iL] * W;
+                } else {
+                    double Wamp3 = Wamp[i] * Wamp[j] * Wamp[k];
+                    double W_re = Wph[2 * (i + j + k)] * Wamp3;
+                    double W_im = Wph[2 * (i + j + k) + 1] * Wamp3;
+                    double f_re = ORE(g, i, j, k);
+                    double f_im = OIM(g, i, j, k);
+                    ORE(g, i, j, k) = Legendre[iL] * (f_re * W_re - f_im * W_im);
+                    OIM(g, i, j, k) = Legendre[iL] * (f_re * W_im + f_im * W_re);
+                }
+            }
+    og_k2x(g, 0);
+    for (int isub = 0; isub < Nsub; ++isub)
+        for (int jsub = 0; jsub < Nsub; ++jsub)
+            for (int ksub = 0; ksub < Nsub; ++ksub)
+                out[(isub * Nsub + jsub) * Nsub + ksub] = OF(g, isub * Ngsub, jsub * Ngsub, ksub * Ngsub) / bias;
+    free(Wamp);
+    free(Wph);
+    free(Kval);
+}

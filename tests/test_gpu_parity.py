@@ -363,3 +363,33 @@ def test_window_deconvolution(fg, oracle_lib, prec, Ng, Nsub, kind):
         np.testing.assert_array_equal(got, want)
     else:
         np.testing.assert_allclose(got, want, rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("prec,Ng,Nsub", [("f64", 16, 2), ("f64", 24, 3), ("f32", 32, 4)])
+@pytest.mark.parametrize("sphere", [0, 1])
+def test_super_sample_modes(fg, oracle_lib, prec, Ng, Nsub, sphere):
+    """fftgal_dl_sub against the loops of src/app/DLsb.c / DLss.c restated in
+    the oracle (og_dl), on a painted uniform catalog, for two lines of sight:
+    FP64 grids to 1e-10 and FP32 grids to 2e-5 of the largest |Delta|."""
+    L = 200.0
+    x, y, z = uniform_box(40 + Ng, 3000, L)
+    V = L ** 3
+    offset = [0.0, 0.0, 0.0] if sphere else [0.5, 0.5, 0.5]
+    los_list = [(0.0, 0.0, 1.0), (1.0, 1.0, 0.0)]
+    g = fg.Grid(Ng, L, precision=prec, host_view="lazy")
+    cat = fg.Catalog(x, y, z, V)
+    g.p2g(cat, offset)
+    g.x2k(0)
+    got = g.dl_sub(sphere, Nsub, los_list)
+    want = np.zeros_like(got)
+    o = oracle_lib.Oracle(Ng, L)
+    for l, los in enumerate(los_list):
+        for iL in range(3):
+            o.p2g(x, y, z, V, offset)
+            o.x2k(0)
+            want[l, iL] = o.dl(sphere, Nsub, los, iL)
+    tol = 1e-10 if prec == "f64" else 2e-5
+    scale = np.abs(want).max()
+    assert scale > 0
+    err = np.abs(got - want).max() / scale
+    assert err <= tol, f"max error {err:.2e} of {scale:.3e}"
