@@ -97,6 +97,8 @@ SIGNATURES = {
     "fftgal_dl_sub": (C.c_int, [_P_F, C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp]),
     "fftgal_power_batch_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp, _dp,
                                          C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
+    "fftgal_power_single_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
+                                          C.c_int, _dp, C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_power_rsd_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_long, C.c_double, C.c_int, _dp, C.c_double, C.c_double,
                                        C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
@@ -343,9 +345,10 @@ class Grid:
         return out
 
     def power_f32(self, x, y, z, V: float, los, dK: float, Nmu: int = 3, where: int = MEM_HOST,
-                  Np: int | None = None) -> dict:
-        """Fused interlaced P_l and wedges of one FP32 catalog.  For
-        ``where=MEM_DEVICE`` pass integer device pointers and ``Np``."""
+                  Np: int | None = None, interlace: bool = True) -> dict:
+        """Fused interlaced P_l and wedges of one FP32 catalog (``interlace=False``:
+        a single paint, fftgal_power_single_f32).  For ``where=MEM_DEVICE`` pass
+        integer device pointers and ``Np``."""
         if where == MEM_HOST:
             xs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
             ptrs = [a.ctypes.data for a in xs]
@@ -360,7 +363,8 @@ class Grid:
         Nm = np.zeros((NK, Nmu), dtype=np.int64)
         Pm = np.zeros((NK, Nmu))
         l = _f64(los)
-        _check(lib().fftgal_power_f32(self.p, ptrs[0], ptrs[1], ptrs[2], int(Np), float(V), int(where),
+        fn = lib().fftgal_power_f32 if interlace else lib().fftgal_power_single_f32
+        _check(fn(self.p, ptrs[0], ptrs[1], ptrs[2], int(Np), float(V), int(where),
                                       l.ctypes.data_as(_dp), float(dK), int(Nmu),
                                       K.ctypes.data_as(_dp), N.ctypes.data_as(_lp), P.ctypes.data_as(_dp),
                                       Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))

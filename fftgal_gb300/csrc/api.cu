@@ -934,14 +934,16 @@ namespace fg {
 // (nullable) displaces every particle along the line of sight while painting
 static int power_f32_run(fft_t *grid, const float *x, const float *y, const float *z, const float *const *vel,
                          double aH, long Np, double V, int where, const double los_in[3], double dK, int Nmu,
-                         double *K, long *N, double *Plout, double *Kmu, long *Nmu_count, double *Pmuout) {
+                         double *K, long *N, double *Plout, double *Kmu, long *Nmu_count, double *Pmuout,
+                         bool interlace = true) {
     if (!grid || !x || !y || !z || Np <= 0 || !(V > 0)) return set_error(ERR_ARG, "fftgal_power_f32: bad arguments");
     if (vel && (!vel[0] || !vel[1] || !vel[2] || !(aH != 0)))
         return set_error(ERR_ARG, "fftgal_power_rsd_f32: bad velocities or aH");
     Grid *g = G(grid);
     if (g->prec != 4) return set_error(ERR_STATE, "fftgal_power_f32 needs an FP32 grid");
-    FG_TRY(ensure_aux(g));
+    if (interlace) FG_TRY(ensure_aux(g));
     FG_TRY(ensure_tables(g));
+    const int ngr = interlace ? 2 : 1;
     const bool tm = g->timing != 0;
     cudaStream_t st = g->stream;
     cudaEvent_t *ev = g->ev;
@@ -991,14 +993,14 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
         spec[1].offset[a] = remainder(0.5, Ng);
     }
     spec[0].scale = spec[1].scale = Npcinv;
-    FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, 2, st, tm ? ev + 2 : nullptr,
+    FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, ngr, st, tm ? ev + 2 : nullptr,
                  vel ? &rsd : nullptr));
     void *grids[2] = {g->d_f, g->d_aux};
-    FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
-    FG_TRY(fft_pass_j(&g->fft, grids, 2, -1, st));
+    FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
-    FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
+    FG_TRY(fft_pass_i(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
     for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
     ++g->version;
@@ -1013,9 +1015,11 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
     fin.B = g->d_aux;
     fin.ph32 = dual_tab32(g);
     fin.w32 = winv_tab32(g);
-    fin.scale = 0.5 * H3;
+    fin.scale = interlace ? 0.5 * H3 : H3;
+    if (!interlace) fin.B = nullptr;
     if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
-    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, 2, Vinv, Pshot, tm ? &ev[10] : nullptr, &fin));
+    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, interlace ? 2 : 3, Vinv, Pshot, tm ? &ev[10] : nullptr,
+                    &fin));
     if (tm) {
         FG_CUDA(cudaEventSynchronize(ev[kStages]));
         float ms;
@@ -1177,6 +1181,13 @@ extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const 
     }
     FG_CUDA(cudaStreamSynchronize(g->copy_stream));
     return OK;
+}
+
+extern "C" int fftgal_power_single_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
+                                       double V, int where, const double los[3], double dK, int Nmu, double *K,
+                                       long *N, double *Pl, double *Kmu, long *Nmu_count, double *Pmu) {
+    return power_f32_run(grid, x, y, z, nullptr, 0, Np, V, where, los, dK, Nmu, K, N, Pl, Kmu, Nmu_count, Pmu,
+                         false);
 }
 
 extern "C" int fftgal_power_rsd_f32(fft_t *grid, const float *x, const float *y, const float *z, const float *vx,

@@ -80,6 +80,68 @@ __device__ __forceinline__ int kbin_est(uint32_t n2, float kamp, const uint32_t 
     return b;
 }
 
+// One thread's run of modes whose k bin changes rarely (a run along the
+// grid axis with the smallest |n_a|): the run's sums of P L_l(mu^2), l = 0, 2,
+// 4, 6, and of P per wedge stay in registers and are added to the CTA's FP32
+// shared accumulators acc32 [4 + W][NK] when the bin or the wedge changes.
+struct BinRun {
+    int cb = -1, cm = -1;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, sw = 0.f;
+
+    __device__ __forceinline__ void flush_bin(float *acc32, int NK) {
+        if (cb >= 0) {
+            atomicAdd(acc32 + 0 * NK + cb, s0);
+            atomicAdd(acc32 + 1 * NK + cb, s1);
+            atomicAdd(acc32 + 2 * NK + cb, s2);
+            atomicAdd(acc32 + 3 * NK + cb, s3);
+            atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
+        }
+    }
+    // mode (ki, kj, kk) of the half spectrum, raw k index kraw (its count is
+    // 1 + (2 kraw % Ng > 0), src/power.c:57), power p; not the k = 0 mode
+    __device__ __forceinline__ void add(const BinDev &d, const uint32_t *thr, float *acc32, int ki, int kj, int kk,
+                                        int kraw, float p) {
+        const int NK = d.NK;
+        const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
+        const float pc = (kraw != 0 && 2 * kraw != d.Ng) ? 2.f * p : p;
+        const float n2f = (float)n2;
+        const float rk = rsqrtf(n2f);
+        int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
+        if (b >= NK) b = -1;
+        float m2;
+        const int imu = wedge_index_r(ki, kj, kk, rk, d, m2);
+        if (b != cb) {
+            flush_bin(acc32, NK);
+            cb = b;
+            cm = imu;
+            s0 = s1 = s2 = s3 = sw = 0.f;
+        } else if (imu != cm) {
+            if (cb >= 0) atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
+            cm = imu;
+            sw = 0.f;
+        }
+        s0 += pc;
+        s1 += pc * (1.5f * m2 - 0.5f);
+        s2 += pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f);
+        s3 += pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f);
+        sw += pc;
+    }
+    __device__ __forceinline__ void finish(const BinDev &d, float *acc32) { flush_bin(acc32, d.NK); }
+};
+
+// fold a CTA's FP32 shared sums [NQ][NK] into the FP64 global sums [NK][NQ]
+// and clear them (every thread of the CTA takes part; the caller synchronises)
+__device__ __forceinline__ void bin_fold(float *acc32, double *gacc, int NK, int NQ) {
+    for (int e = threadIdx.x; e < NK * NQ; e += blockDim.x) {
+        const float v = acc32[e];
+        if (v != 0.f) {
+            const int q = e / NK, b = e - q * NK;
+            atomicAdd(&gacc[(size_t)b * NQ + q], (double)v);
+            acc32[e] = 0.f;
+        }
+    }
+}
+
 static inline BinDev make_dev(const BinSpec &s) {
     BinDev d;
     d.Ng = s.Ng;

@@ -298,6 +298,8 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
 //   MODE 1: the grid holds delta; P = |delta|^2 Vinv - Pshot.
 //   MODE 2: as 1, with the interlacing finish of the grid fused in: A <-
 //           (A + B * phase) * W^-1 * scale is written back and binned.
+//   MODE 3: as 2 without an interlacing grid: A <- A * W^-1 * scale (the
+//           deconvolution of a single paint, src/fft.c:236-254).
 constexpr int kSlabI = 16, kSlabJ = 16, kSlabK = 32, kSlabRow = 33;
 constexpr int kSlabThreads = 512;  // one warp per slab of a block
 constexpr int kFoldBlocks = 8;
@@ -344,8 +346,8 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
         if (fixed < Ng) {
             float2 pfk = make_float2(0.f, 0.f);
             float wfk = 0.f;
-            if (MODE == 2 && k < nh) {
-                pfk = cmul(fin.ph[(rows_i ? Ng : 0) + fixed], fin.ph[2 * Ng + k]);
+            if (MODE >= 2 && k < nh) {
+                if (MODE == 2) pfk = cmul(fin.ph[(rows_i ? Ng : 0) + fixed], fin.ph[2 * Ng + k]);
                 wfk = fin.w[fixed] * fin.w[k] * fin.scale;
             }
 #pragma unroll 4
@@ -360,6 +362,12 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
                         const float2 bv = fin.B[e], av = fin.A[e];
                         const float2 dv = cmul(bv, p);
                         const float2 v = make_float2((dv.x + av.x) * wk, (dv.y + av.y) * wk);
+                        fin.A[e] = v;
+                        pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+                    } else if (MODE == 3) {
+                        const float wk = wfk * fin.w[rr];
+                        const float2 av = fin.A[e];
+                        const float2 v = make_float2(av.x * wk, av.y * wk);
                         fin.A[e] = v;
                         pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
                     } else if (MODE == 1) {
@@ -377,65 +385,21 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
             // runs along k: lane = (row, half of the 32 k); else lane = k
             int r = axis == 2 ? (lane & 15) : 0, c = axis == 2 ? 16 * (lane >> 4) : lane;
             const int dr = axis == 2 ? 0 : 1, dc = axis == 2 ? 1 : 0;
-            int cb = -1, cm = -1;
-            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, sw = 0.f;
+            BinRun run;
             for (int t = 0; t < 16; ++t, r += dr, c += dc) {
                 const int rr = r0 + r, kc = k0 + c;
                 if (rr >= Ng || kc >= nh) continue;
                 const int i = rows_i ? rr : fixed, j = rows_i ? fixed : rr;
                 if ((i | j | kc) == 0) continue;  // the k = 0 mode (src/power.c:52-54)
-                const int ki = kval(i, Ng), kj = kval(j, Ng), kk = kval(kc, Ng);
-                const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
-                const float p = slab[r * kSlabRow + c];
-                const float pc = (kc != 0 && 2 * kc != Ng) ? 2.f * p : p;  // count 1 + (2k % Ng > 0)
-                const float n2f = (float)n2;
-                const float rk = rsqrtf(n2f);
-                int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
-                if (b >= NK) b = -1;
-                float m2;
-                const int imu = wedge_index_r(ki, kj, kk, rk, d, m2);
-                if (b != cb) {
-                    if (cb >= 0) {
-                        atomicAdd(acc32 + 0 * NK + cb, s0);
-                        atomicAdd(acc32 + 1 * NK + cb, s1);
-                        atomicAdd(acc32 + 2 * NK + cb, s2);
-                        atomicAdd(acc32 + 3 * NK + cb, s3);
-                        atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
-                    }
-                    cb = b;
-                    cm = imu;
-                    s0 = s1 = s2 = s3 = sw = 0.f;
-                } else if (imu != cm) {
-                    if (cb >= 0) atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
-                    cm = imu;
-                    sw = 0.f;
-                }
-                s0 += pc;
-                s1 += pc * (1.5f * m2 - 0.5f);
-                s2 += pc * ((4.375f * m2 - 3.75f) * m2 + 0.375f);
-                s3 += pc * (((14.4375f * m2 - 19.6875f) * m2 + 6.5625f) * m2 - 0.3125f);
-                sw += pc;
+                run.add(d, thr, acc32, kval(i, Ng), kval(j, Ng), kval(kc, Ng), kc, slab[r * kSlabRow + c]);
             }
-            if (cb >= 0) {
-                atomicAdd(acc32 + 0 * NK + cb, s0);
-                atomicAdd(acc32 + 1 * NK + cb, s1);
-                atomicAdd(acc32 + 2 * NK + cb, s2);
-                atomicAdd(acc32 + 3 * NK + cb, s3);
-                atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
-            }
+            run.finish(d, acc32);
         }
         __syncwarp();
         if (++since_fold == kFoldBlocks) {
             since_fold = 0;
             __syncthreads();
-            for (int e = tid; e < NK * NQ; e += blockDim.x) {
-                const float v = acc32[e];
-                if (v != 0.f) {
-                    const int q = e / NK, b = e - q * NK;
-                    atomicAdd(&gacc[(size_t)b * NQ + q], (double)v);
-                    acc32[e] = 0.f;
-                }
-            }
+            bin_fold(acc32, gacc, NK, NQ);
             __syncthreads();
         }
     }
@@ -457,7 +421,7 @@ static size_t slab_smem(int NK, int NQ) {
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
               double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end, const BinFinish *fin) {
     if (!g->valid) return set_error(ERR_STATE, "bin geometry not built");
-    if (mode == 2 && (prec != 4 || !fin)) return set_error(ERR_ARG, "fused finish needs an FP32 grid");
+    if (mode >= 2 && (prec != 4 || !fin)) return set_error(ERR_ARG, "fused finish needs an FP32 grid");
     const BinSpec &s = g->spec;
     const BinDev d = make_dev(s);
     const int NK = s.NK, W = s.Nmu + 1, NQ = 4 + W;
@@ -479,7 +443,7 @@ int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, do
             sf.w = static_cast<const float *>(fin->w32);
             sf.scale = (float)fin->scale;
         }
-        const float2 *fv = static_cast<const float2 *>(mode == 2 ? fin->A : f);
+        const float2 *fv = static_cast<const float2 *>(mode >= 2 ? fin->A : f);
 #define FG_SLAB_LAUNCH(M)                                                                                   \
     do {                                                                                                    \
         FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
@@ -491,8 +455,10 @@ int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, do
             FG_SLAB_LAUNCH(0);
         else if (mode == 1)
             FG_SLAB_LAUNCH(1);
-        else
+        else if (mode == 2)
             FG_SLAB_LAUNCH(2);
+        else
+            FG_SLAB_LAUNCH(3);
 #undef FG_SLAB_LAUNCH
     } else {
         const int Ng_pad = 2 * (s.Ng / 2 + 1);

@@ -122,6 +122,16 @@ int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const f
                            const double los[3], double dK, int Nmu, double *K, long *N,
                            double *Pl, double *Kmu, long *Nmu_count, double *Pmu);
 
+/* fftgal_power_f32 without interlacing: one paint, r2c, PCS deconvolution,
+ * multipoles and wedges -- the sequence fft_p2g(offset 0) -> fft_x2k(0) ->
+ * fft_deconv -> P -> Pl -> Pmu (src/fft.c:57-131,172-181,236-254,
+ * src/power.c:12-178).  Half the paint and FFT work of the interlaced call;
+ * aliasing is not suppressed. */
+int fftgal_power_single_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
+                            double V, int where, const double los[3], double dK, int Nmu,
+                            double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
+                            double *Pmu);
+
 /* fftgal_power_f32 of the redshift-space catalog: every particle is
  * displaced along the line of sight while it is painted, x + (v . los) / aH
  * los, as gal_rsd forms it (src/gal.c:63-77), so the P.c sequence

@@ -88,3 +88,17 @@ def test_rsd_fused_into_paint(fg, oracle_lib, real_space, los, aH):
     xs, ys, zs = oracle_lib.Oracle.rsd(x, y, z, vx, vy, vz, los, aH)
     want = oracle_lib.power_spectrum(Ng, Lfd, xs, ys, zs, los, dK, Nmu=Nmu, V=V)
     _check(got, want, V / len(x), 0.8 * np.pi * Ng / Lfd)
+
+
+@pytest.mark.parametrize("fold", [1, 4])
+def test_single_paint_against_oracle(fg, oracle_lib, catalog, fold):
+    """fftgal_power_single_f32 (no interlacing) against the oracle's
+    fft_p2g -> fft_x2k -> fft_deconv -> P -> Pl -> Pmu on the clustered catalog."""
+    L, (x, y, z) = catalog
+    Ng, Lfd, Nmu = 128, L / fold, 10
+    los, dK, V = (0.0, 0.0, 1.0), 2 * np.pi / Lfd, L ** 3
+    g = fg.Grid(Ng, Lfd, precision="f32", host_view="lazy")
+    got = g.power_f32(x, y, z, V, los, dK, Nmu=Nmu, interlace=False)
+    want = oracle_lib.power_spectrum(Ng, Lfd, x, y, z, los, dK, Nmu=Nmu, V=V, interlace=False)
+    assert want["status"] == (0, 0)
+    _check(got, want, V / len(x), 0.8 * np.pi * Ng / Lfd)
