@@ -97,6 +97,17 @@ SIGNATURES = {
     "fftgal_dl_sub": (C.c_int, [_P_F, C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp]),
     "fftgal_power_batch_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp, _dp,
                                          C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
+    "fftgal_mlp_nparams": (C.c_int, []),
+    "fftgal_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
+    "fftgal_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float,
+                                  C.c_void_p]),
+    "fftgal_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]),
+    "fftgal_alias_features": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, C.POINTER(C.c_float)]),
+    "fftgal_alias_envelope": (C.c_double, [C.c_double]),
+    "fftgal_power_learned_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
+                                           C.c_int, _dp, C.c_double, C.c_int, C.POINTER(C.c_float), _dp, _lp,
+                                           _dp, _dp, _lp, _dp]),
     "fftgal_power_single_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                           C.c_int, _dp, C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_power_rsd_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -298,6 +309,12 @@ class Grid:
         _check(lib().fftgal_sync_device(self.p))
 
     def set_stream(self, stream_ptr: int | None):
+        """Run the grid's work on a CUDA stream: None for the library's own
+        stream, else a cudaStream_t.  0, torch's handle of the legacy default
+        stream, is passed as cudaStreamLegacy (the C API reads NULL as the
+        library's own stream)."""
+        if stream_ptr == 0:
+            stream_ptr = 1  # cudaStreamLegacy
         _check(lib().fftgal_set_stream(self.p, stream_ptr))
 
     def set_timing(self, on: bool):

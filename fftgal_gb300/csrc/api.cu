@@ -16,6 +16,7 @@
 #include "power.h"
 #include "fftgal_gb300.h"
 
+#include <cmath>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -1188,6 +1189,49 @@ extern "C" int fftgal_power_single_f32(fft_t *grid, const float *x, const float 
                                        long *N, double *Pl, double *Kmu, long *Nmu_count, double *Pmu) {
     return power_f32_run(grid, x, y, z, nullptr, 0, Np, V, where, los, dK, Nmu, K, N, Pl, Kmu, Nmu_count, Pmu,
                          false);
+}
+
+extern "C" int fftgal_power_learned_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
+                                        double V, int where, const double los[3], double dK, int Nmu,
+                                        const float *mlp_params, double *K, long *N, double *Pl, double *Kmu,
+                                        long *Nmu_count, double *Pmu) {
+    if (!mlp_params) return set_error(ERR_ARG, "fftgal_power_learned_f32: no MLP parameters");
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    const int NK = fftgal_nk(grid->Ng, grid->L, dK);
+    if (NK < 1) return set_error(ERR_ARG, "fftgal_power_learned_f32: bad dK");
+    std::vector<double> Kb(NK), Pb((size_t)NK * 4);
+    std::vector<long> Nb(NK);
+    FG_TRY(power_f32_run(grid, x, y, z, nullptr, 0, Np, V, where, los, dK, Nmu, Kb.data(), Nb.data(), Pb.data(), Kmu,
+                         Nmu_count, Pmu, false));
+    const double Pshot = V / Np, kNyq = M_PI * grid->Ng / grid->L;
+    const int np = fftgal_mlp_nparams();
+    std::vector<float> X((size_t)NK * 5), Y((size_t)NK * 3);
+    FG_TRY(fftgal_alias_features(NK, Kb.data(), Pb.data(), Pshot, kNyq, X.data()));
+    Grid *g = G(grid);
+    float *d = nullptr;
+    FG_CUDA(cudaMalloc(&d, sizeof(float) * ((size_t)np + X.size() + Y.size())));
+    float *dp = d, *dx = d + np, *dy = dx + X.size();
+    cudaError_t e = cudaMemcpyAsync(dp, mlp_params, sizeof(float) * np, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, X.data(), sizeof(float) * X.size(), cudaMemcpyHostToDevice, g->stream);
+    int rc = cuda_check(e, "fftgal_power_learned_f32 upload");
+    if (rc == OK) rc = fftgal_mlp_forward(dp, dx, NK, dy, g->stream);
+    if (rc == OK)
+        rc = cuda_check(cudaMemcpyAsync(Y.data(), dy, sizeof(float) * Y.size(), cudaMemcpyDeviceToHost, g->stream),
+                        "fftgal_power_learned_f32 download");
+    if (rc == OK) rc = cuda_check(cudaStreamSynchronize(g->stream), "fftgal_power_learned_f32");
+    cudaFree(d);
+    FG_TRY(rc);
+    // P_l += den e(k / k_Nyq) y_l (l = 0, 2, 4) on bins with modes; l = 6 as measured
+    for (int b = 0; b < NK; ++b) {
+        if (K) K[b] = Kb[b];
+        if (N) N[b] = Nb[b];
+        const double den = fabs(Pb[4 * b]) + Pshot;
+        const bool ok = std::isfinite(Pb[4 * b]) && Nb[b] > 0;
+        const double sc = ok ? den * fftgal_alias_envelope(Kb[b] / kNyq) : 0.0;
+        for (int l = 0; l < 4; ++l)
+            if (Pl) Pl[4 * b + l] = Pb[4 * b + l] + (l < 3 ? sc * Y[3 * b + l] : 0.0);
+    }
+    return OK;
 }
 
 extern "C" int fftgal_power_rsd_f32(fft_t *grid, const float *x, const float *y, const float *z, const float *vx,

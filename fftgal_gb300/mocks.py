@@ -23,9 +23,9 @@ def pk_model(k, amp: float = 1e4, slope: float = -1.5):
 
 
 def lognormal_catalog(n: int, L: float, Np: float, seed: int, f: float = 0.8, slope: float = -1.5,
-                      amp: float = 1e4, device=None):
+                      amp: float = 1e4, device=None, axes=(0, 1, 2)):
     """x, y, z, vx, vy, vz as FP32 tensors on ``device`` (default cuda) with
-    about Np particles."""
+    about Np particles; velocity components not in ``axes`` are left None."""
     import torch
     dev = torch.device(device) if device is not None else torch.device("cuda")
     gen = torch.Generator(device=dev)
@@ -58,7 +58,10 @@ def lognormal_catalog(n: int, L: float, Np: float, seed: int, f: float = 0.8, sl
     z = ((ck.to(torch.float64) + torch.rand(tot, generator=gen, device=dev, dtype=torch.float64)) * H)
     inv = torch.where(k2 > 0, 1.0 / torch.clamp(k2, min=1e-300), torch.zeros_like(k2)).to(torch.float32)
     vel = []
-    for kc in (kx, ky, kzz):
+    for a, kc in enumerate((kx, ky, kzz)):
+        if a not in axes:
+            vel.append(None)
+            continue
         psi = torch.fft.irfftn(1j * kc.to(torch.float32) * inv * gk, s=(n, n, n))
         vel.append((f * psi.reshape(-1)[cell]).to(torch.float32))
         del psi

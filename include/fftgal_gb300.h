@@ -132,6 +132,37 @@ int fftgal_power_single_f32(fft_t *grid, const float *x, const float *y, const f
                             double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
                             double *Pmu);
 
+/* Learned aliasing correction (no counterpart in the reference): a
+ * 5 -> 64 -> 64 -> 64 -> 3 tanh perceptron, FP32, mapping the single-paint
+ * multipoles of a k bin to the interlaced ones.  Features of bin b (den =
+ * |P0| + Pshot): k / k_Nyq, Pshot / den, P2 / den, P4 / den and the local
+ * slope d ln den / d ln k; outputs (P_l^interlaced - P_l^single) / den, l = 0,
+ * 2, 4.  Parameters: fftgal_mlp_nparams() floats, W1[5][64] b1 W2[64][64] b2
+ * W3[64][64] b3 W4[64][3] b4.  The training and forward kernels take device
+ * pointers; fftgal_mlp_grad accumulates into grad and loss (the caller clears
+ * them) the gradient and value of the mean squared error over n samples
+ * (X[n][5], T[n][3]); fftgal_mlp_adam takes one Adam step (beta 0.9, 0.999). */
+int fftgal_mlp_nparams(void);
+int fftgal_mlp_grad(const float *params, const float *X, const float *T, long n, float *grad,
+                    float *loss, void *stream);
+int fftgal_mlp_adam(float *params, const float *grad, float *m, float *v, int step, float lr,
+                    void *stream);
+int fftgal_mlp_forward(const float *params, const float *X, long n, float *Y, void *stream);
+/* features X[NK][5] of single-paint multipoles P[NK][4] (host arrays; empty
+ * bins give zeros) */
+int fftgal_alias_features(int NK, const double *K, const double *P, double Pshot, double kNyq,
+                          float *X);
+/* e(u) = u^6 / (1 + u^6), u = k / k_Nyq: the scale of the perceptron's
+ * outputs, P_l^interlaced - P_l^single = (|P0| + Pshot) e(u) y_l */
+double fftgal_alias_envelope(double u);
+/* fftgal_power_single_f32 with P_0,2,4 corrected by the perceptron with host
+ * parameters mlp_params (wedges and P_6 as measured): one paint and one FFT
+ * instead of two of each. */
+int fftgal_power_learned_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
+                             double V, int where, const double los[3], double dK, int Nmu,
+                             const float *mlp_params, double *K, long *N, double *Pl, double *Kmu,
+                             long *Nmu_count, double *Pmu);
+
 /* fftgal_power_f32 of the redshift-space catalog: every particle is
  * displaced along the line of sight while it is painted, x + (v . los) / aH
  * los, as gal_rsd forms it (src/gal.c:63-77), so the P.c sequence

@@ -85,3 +85,53 @@ def test_reference_drivers_link_unchanged(built, tmp_path, app):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert out.exists()
+
+
+def test_alias_features_definition():
+    """fftgal_alias_features (host code) against its definition: k/k_Nyq,
+    Pshot/den, P2/den, P4/den, d ln den / d ln k over the neighbouring bins
+    with modes (one-sided at the ends, clamped to [-5, 5]); empty bins give
+    zeros."""
+    import numpy as np
+    from fftgal_gb300 import alias_mlp as a
+    rng = np.random.default_rng(1)
+    NK = 12
+    K = np.sort(rng.uniform(0.01, 0.5, NK))
+    P = rng.normal(0, 50, (NK, 4))
+    P[:, 0] = rng.uniform(10, 1000, NK)
+    P[4] = np.nan  # an empty bin
+    Pshot, kN = 20.0, 0.4
+    X = a.features(K, P, Pshot, kN)
+    ok = np.isfinite(P[:, 0])
+    den = np.abs(P[:, 0]) + Pshot
+    for b in range(NK):
+        if not ok[b]:
+            assert np.all(X[b] == 0)
+            continue
+        lo = b - 1
+        while lo >= 0 and not ok[lo]:
+            lo -= 1
+        hi = b + 1
+        while hi < NK and not ok[hi]:
+            hi += 1
+        lo = b if lo < 0 else lo
+        hi = b if hi >= NK else hi
+        slope = 0.0 if hi == lo else (np.log(den[hi]) - np.log(den[lo])) / (np.log(K[hi]) - np.log(K[lo]))
+        want = [K[b] / kN, Pshot / den[b], P[b, 1] / den[b], P[b, 2] / den[b], np.clip(slope, -5, 5)]
+        np.testing.assert_allclose(X[b], want, rtol=1e-6, atol=1e-7)
+
+
+def test_alias_envelope_and_scaled_targets():
+    """fftgal_alias_envelope is u^6 / (1 + u^6), and the trainer's targets are
+    the raw ones over it, clipped to +-5."""
+    import numpy as np
+    from fftgal_gb300 import alias_mlp as a, lib
+    for u in (0.0, 0.1, 0.5, 1.0, 1.7):
+        assert abs(lib().fftgal_alias_envelope(u) - u ** 6 / (1 + u ** 6)) <= 1e-15
+    X = np.zeros((3, a.IN), dtype=np.float32)
+    X[:, 0] = [0.5, 1.0, 1.5]
+    T = np.array([[1e-3, -1e-3, 0], [0.1, 0.2, -20], [100, 0, 0]], dtype=np.float32)
+    S = a.scaled_targets(X, T)
+    e = a.envelope(X[:, 0].astype(np.float64))
+    np.testing.assert_allclose(S, np.clip(T / e[:, None], -5, 5), rtol=1e-6)
+    assert S[1, 2] == -5 and S[2, 0] == 5

@@ -41,3 +41,23 @@ def test_mocks_match_numpy_generator(fg):
     ratio = np.mean(p_gpu, axis=0)[sel] / np.mean(p_np, axis=0)[sel]
     assert np.all(np.abs(ratio - 1) < 0.2), ratio
     assert abs(np.mean(v_gpu) / np.mean(v_np) - 1) < 0.1
+
+
+def test_device_catalog_ordered_after_torch_stream(fg):
+    """A catalog written by torch kernels and measured through device pointers
+    on a grid bound to torch's current stream (handle 0, the legacy default
+    stream), with no synchronisation in between, gives the host-path result."""
+    import torch
+    from fftgal_gb300 import mocks
+    n, L, Np = 64, 1000.0, 4e5
+    dK = 2 * np.pi / L
+    g = fg.Grid(n, L, precision="f32", host_view="lazy")
+    g.set_stream(torch.cuda.current_stream().cuda_stream)
+    for seed in (11, 12):
+        x, y, z, vx, vy, vz = mocks.lognormal_catalog(n, L, Np, seed, axes=(2,))
+        zr = (z + vz).contiguous()
+        rd = g.power_f32(x.data_ptr(), y.data_ptr(), zr.data_ptr(), L ** 3, (0, 0, 1), dK, Nmu=3,
+                         where=fg.MEM_DEVICE, Np=int(x.numel()))
+        rh = g.power_f32(x.cpu().numpy(), y.cpu().numpy(), zr.cpu().numpy(), L ** 3, (0, 0, 1), dK, Nmu=3)
+        ok = rh["N"] > 0
+        np.testing.assert_allclose(rd["P"][ok], rh["P"][ok], rtol=1e-5, atol=1e-3)
