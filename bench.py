@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--np", type=float, default=NP)
     ap.add_argument("--mock", default="uniform", choices=["uniform", "lognormal"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plan", default=None,
+                    help="plan file of the FFT autotuner (default: one in the temporary directory)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only warmup+this many steps, no e2e/cpu legs (for ncu)")
     return ap.parse_args()
@@ -251,7 +253,10 @@ def run_ours(args):
 
     pos = make_catalog(torch, Np, 1234 + rank, args.mock, dev)
     Np = int(pos.shape[1])
-    grid = fg.Grid(Ng, L_BOX, precision="f32", host_view="lazy")
+    # the FFT launch shapes come from the autotuner's plan file (measured on
+    # the first run on a device, like FFTW_MEASURE wisdom)
+    plan = args.plan or os.path.join(tempfile.gettempdir(), f"fftgal_gb300_plan_rank{local}.txt")
+    grid = fg.Grid(Ng, L_BOX, wisdom=plan, precision="f32", host_view="lazy")
     grid.set_stream(stream.cuda_stream)
     xp, yp, zp = (pos[a].data_ptr() for a in range(3))
 
@@ -354,6 +359,8 @@ def run_ours(args):
                        "Ng": Ng, "Np": Np, "los": LOS, "mock": args.mock,
                        "l2": "inputs larger than L2 (two 4.3 GB grids per step)",
                        "parallelism": f"replicas x{world}",
+                       "fft_plan": {"source": ["built-in", "measured", "plan file", "process cache"][
+                           grid.plan_info()["source"]], "tune": grid.plan_info()["tune"]},
                        "stages_ms": stage_table,
                        "step_roofline": {"algorithmic_bytes": step_algo,
                                          "achieved_GBs": round(step_algo / (ms / args.steps / 1000) / 1e9, 1),

@@ -26,6 +26,7 @@ _lp = C.POINTER(C.c_long)
 
 VIEW_SYNC, VIEW_LAZY = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
+PLAN_BUILTIN, PLAN_MEASURED, PLAN_FILE, PLAN_CACHE = 0, 1, 2, 3
 
 
 class FFT_T(C.Structure):
@@ -105,6 +106,12 @@ SIGNATURES = {
     "fftgal_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]),
     "fftgal_alias_features": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, C.POINTER(C.c_float)]),
     "fftgal_alias_envelope": (C.c_double, [C.c_double]),
+    "fftgal_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
+    "fftgal_plan_autotune": (C.c_int, [C.c_void_p, _dp]),
+    "fftgal_plan_lookup": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "fftgal_plan_store": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), _dp,
+                                    C.c_char_p]),
+    "fftgal_plan_valid": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "fftgal_power_learned_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                            C.c_int, _dp, C.c_double, C.c_int, C.POINTER(C.c_float), _dp, _lp,
                                            _dp, _dp, _lp, _dp]),
@@ -307,6 +314,22 @@ class Grid:
 
     def sync_device(self):
         _check(lib().fftgal_sync_device(self.p))
+
+    def plan_info(self) -> dict:
+        """Launch shapes of the FFT passes (fftgal_plan_info): ``tune`` = [k rows
+        per CTA, j and i log2 columns per CTA], ``source`` (FFTGAL_PLAN_*) and
+        the measured ms of each pass."""
+        t = (C.c_int * 3)()
+        src = C.c_int()
+        ms = np.zeros(3)
+        _check(lib().fftgal_plan_info(self.p, t, C.byref(src), ms.ctypes.data_as(_dp)))
+        return {"tune": list(t), "source": src.value, "ms": ms}
+
+    def autotune(self) -> np.ndarray:
+        """Measure the FFT launch shapes now (clears the grid)."""
+        ms = np.zeros(3)
+        _check(lib().fftgal_plan_autotune(self.p, ms.ctypes.data_as(_dp)))
+        return ms
 
     def set_stream(self, stream_ptr: int | None):
         """Run the grid's work on a CUDA stream: None for the library's own

@@ -112,6 +112,8 @@ struct Grid {
     int timing = 0;
     cudaEvent_t ev[kStages + 1] = {};
     double stage_ms[kStages + 1] = {};
+    int plan_source = FFTGAL_PLAN_BUILTIN;
+    double plan_ms[3] = {0, 0, 0};
 };
 
 static Grid *G(const fft_t *f) { return f ? reinterpret_cast<Grid *>(f->x2k) : nullptr; }
@@ -399,23 +401,10 @@ extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
     FG_API(fft_plan_create(&g->fft, Ng, g->prec), "fft_init()");
     FG_API(paint_tiling_create(&g->tiling, Ng), "fft_init()");
     FG_API(cuda_check(cudaStreamSynchronize(g->stream), "init"), "fft_init()");
-    const bool estimate = wisdom && !strcmp(wisdom, "FFTW_ESTIMATE");
-    if (estimate) {
+    if (!wisdom || !strcmp(wisdom, "FFTW_ESTIMATE")) {
         fprintf(stderr, "fft_init() using built-in GPU plans (%s grid)\n", g->prec == 4 ? "FP32" : "FP64");
-    } else if (wisdom) {
-        FILE *fp = fopen(wisdom, "r");
-        if (fp) {
-            fclose(fp);
-            fprintf(stderr, "fft_init() found plan file %s\n", wisdom);
-        } else {
-            fp = fopen(wisdom, "w");
-            if (fp) {
-                fprintf(fp, "fftgal_gb300 plan Ng=%d prec=%d cols=%d rows=%d tile=%dx%dx%d\n", Ng, g->prec,
-                        g->fft.cols, g->fft.rows, g->tiling.tmax[0], g->tiling.tmax[1], g->tiling.tmax[2]);
-                fclose(fp);
-                fprintf(stderr, "fft_init() exported plan to %s\n", wisdom);
-            }
-        }
+    } else {
+        FG_API(plan_resolve(&g->fft, g->d_f, g->stream, wisdom, false, &g->plan_source, g->plan_ms), "fft_init()");
     }
     return self;
 }
@@ -873,6 +862,31 @@ extern "C" int fftgal_set_stream(fft_t *grid, void *stream) {
     Grid *g = G(grid);
     FG_CUDA(cudaStreamSynchronize(g->stream));
     g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+    return OK;
+}
+
+extern "C" int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms[3]) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    for (int w = 0; w < 3; ++w) {
+        if (tune) tune[w] = g->fft.tune[w];
+        if (ms) ms[w] = g->plan_ms[w];
+    }
+    if (source) *source = g->plan_source;
+    return OK;
+}
+
+extern "C" int fftgal_plan_autotune(fft_t *grid, double ms[3]) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    double t[3];
+    FG_TRY(fft2_autotune(&g->fft, g->d_f, g->stream, t));
+    g->plan_source = FFTGAL_PLAN_MEASURED;
+    for (int w = 0; w < 3; ++w) {
+        g->plan_ms[w] = t[w];
+        if (ms) ms[w] = t[w];
+    }
+    ++g->version;
     return OK;
 }
 

@@ -510,7 +510,8 @@ static void launch_k(bool forward, dim3 grid, const FftPlan *p, void *g0, void *
 
 static int k_pass(const FftPlan *p, void *const *grids, int ngrids, bool forward, cudaStream_t s) {
     if (forward && fft2_supported(p->Ng, p->prec))
-        return fft2_k_r2c(p->Ng, p->half.tw, p->rtw, grids[0], ngrids > 1 ? grids[1] : grids[0], ngrids, s);
+        return fft2_k_r2c(p->Ng, p->half.tw, p->rtw, grids[0], ngrids > 1 ? grids[1] : grids[0], ngrids, s,
+                          p->tune[0]);
     const long nrows = (long)p->Ng * p->Ng;
     const Fft1dPlan &kp = p->even ? p->half : p->axis;
     const Fft1dDev d = to_dev(kp);
@@ -541,10 +542,10 @@ static void launch_cols(dim3 grid, const FftPlan *p, void *g0, void *g1, long el
 }
 
 static int cols_pass(const FftPlan *p, void *const *grids, int ngrids, int sign,
-                     long elem_stride, long batch_stride, cudaStream_t s) {
+                     long elem_stride, long batch_stride, cudaStream_t s, int logC) {
     if (fft2_supported(p->Ng, p->prec))
         return fft2_cols(p->Ng, p->axis.tw, grids[0], ngrids > 1 ? grids[1] : grids[0], ngrids, p->nh,
-                         elem_stride, batch_stride, p->Ng, sign, s);
+                         elem_stride, batch_stride, p->Ng, sign, s, logC);
     const Fft1dDev d = to_dev(p->axis);
     const long ncb = ceil_div(p->nh, p->cols);
     dim3 grid((unsigned)(ncb * p->Ng), ngrids);
@@ -562,11 +563,11 @@ static int cols_pass(const FftPlan *p, void *const *grids, int ngrids, int sign,
 }
 
 int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s) {
-    return cols_pass(p, grids, ngrids, sign, p->nh, (long)p->Ng * p->nh, s);
+    return cols_pass(p, grids, ngrids, sign, p->nh, (long)p->Ng * p->nh, s, p->tune[1]);
 }
 
 int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s) {
-    return cols_pass(p, grids, ngrids, sign, (long)p->Ng * p->nh, p->nh, s);
+    return cols_pass(p, grids, ngrids, sign, (long)p->Ng * p->nh, p->nh, s, p->tune[2]);
 }
 
 int fft_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s) {

@@ -233,21 +233,67 @@ bool fft2_supported(int Ng, int prec) {
         return OK;                                                                                         \
     }
 
+// C columns per CTA: threads = C*N2 around 256, C >= 8 for 64-byte rows;
+// along a widely strided axis (the i pass) C = 16, so every row access is a
+// 128-byte run (measured 15 % faster at Ng = 1024; the j pass is faster with
+// C = 8 and two CTAs per SM)
+static int cols_default_logC(int N2, bool wide) {
+    int logC = wide ? 4 : 3;
+    while ((1 << logC) * N2 < 256 && logC < 5) ++logC;
+    while ((1 << logC) * N2 > 512 && logC > 0) --logC;
+    return logC;
+}
+
+static size_t cols_smem(int N1, int N2, int logC) { return (size_t)N2 * (N1 * (1 << logC) + 8) * sizeof(float2); }
+
+static int k_default_rows(int N2) {
+    int R = 1;  // rows per CTA: threads = R*N2 around 64 (small CTAs, many per SM)
+    while (R * N2 < 64 && R < 64) R *= 2;
+    return R;
+}
+
+static size_t k_smem(int N1, int N2, int R) {
+    const int M = N1 * N2, P = N2 * (N1 + 1), P2 = M + 1;
+    return (size_t)R * (P > P2 ? P : P2) * sizeof(float2);
+}
+
+bool fft2_valid_shape(int Ng, int which, int v) {
+    int N1, N2;
+    const int N = which == 0 ? Ng / 2 : Ng;
+    if (!fft2_supported(Ng, 4) || !split2(N, &N1, &N2)) return false;
+    if (which == 0) {  // k pass: R rows per CTA
+        if (v < 1 || v > 64 || (v & (v - 1))) return false;
+        const int thr = v * N2;
+        return thr >= 32 && thr <= 512 && k_smem(N1, N2, v) <= (size_t)device_max_smem();
+    }
+    if (v < 0 || v > 5) return false;  // j or i pass: log2 columns per CTA
+    const int thr = (1 << v) * N2;
+    return thr >= 32 && thr <= 512 && cols_smem(N1, N2, v) <= (size_t)device_max_smem();
+}
+
+int fft2_default_shape(int Ng, int which) {
+    int N1, N2;
+    if (!split2(which == 0 ? Ng / 2 : Ng, &N1, &N2)) return -1;
+    if (which == 0) return k_default_rows(N2);
+    const long es = which == 1 ? (long)(Ng / 2 + 1) : (long)Ng * (Ng / 2 + 1);
+    return cols_default_logC(N2, es * (long)sizeof(float2) > (1L << 20));
+}
+
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
-              long nbatch, int sign, cudaStream_t s) {
+              long nbatch, int sign, cudaStream_t s, int logC_req) {
     FG_TRY(ensure_w32());
     int N1, N2;
     if (!split2(N, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_cols: N=%d", N);
-    // C columns per CTA: threads = C*N2 around 256, C >= 8 for 64-byte rows;
-    // along a widely strided axis (the i pass) C = 16, so every row access
-    // is a 128-byte run (measured 15 % faster at Ng = 1024; the j pass is
-    // faster with C = 8 and two CTAs per SM)
-    int logC = es * (long)sizeof(float2) > (1L << 20) ? 4 : 3;
-    while ((1 << logC) * N2 < 256 && logC < 5) ++logC;
-    while ((1 << logC) * N2 > 512 && logC > 0) --logC;
+    int logC = cols_default_logC(N2, es * (long)sizeof(float2) > (1L << 20));
+    if (logC_req >= 0) {
+        const int thr = (1 << logC_req) * N2;
+        if (logC_req > 5 || thr < 32 || thr > 512 || cols_smem(N1, N2, logC_req) > (size_t)device_max_smem())
+            return set_error(ERR_ARG, "fft2_cols: %d columns per CTA invalid for N=%d", 1 << logC_req, N);
+        logC = logC_req;
+    }
     const int C = 1 << logC;
     const int threads = C * N2;
-    const size_t smem = (size_t)N2 * (N1 * C + 8) * sizeof(float2);
+    const size_t smem = cols_smem(N1, N2, logC);
     const long ncb = ceil_div(ncols, C);
     dim3 grid((unsigned)(ncb * nbatch), ngrids);
     FG_COLS_CASE(1, 1)
@@ -275,18 +321,21 @@ int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, l
         return OK;                                                                                         \
     }
 
-int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s) {
+int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s, int R_req) {
     FG_TRY(ensure_w32());
     const int M = Ng / 2;
     int N1, N2;
     if (!split2(M, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_k_r2c: Ng=%d", Ng);
     const int Ng_pad = 2 * (M + 1);
     const long nrows = (long)Ng * Ng;
-    int R = 1;  // rows per CTA: threads = R*N2 around 64 (small CTAs, many per SM)
-    while (R * N2 < 64 && R < 64) R *= 2;
+    int R = k_default_rows(N2);
+    if (R_req > 0) {
+        if (!fft2_valid_shape(Ng, 0, R_req))
+            return set_error(ERR_ARG, "fft2_k_r2c: %d rows per CTA invalid for Ng=%d", R_req, Ng);
+        R = R_req;
+    }
     const int threads = R * N2;
-    const int P = N2 * (N1 + 1), P2 = M + 1;
-    const size_t smem = (size_t)R * (P > P2 ? P : P2) * sizeof(float2);
+    const size_t smem = k_smem(N1, N2, R);
     dim3 grid((unsigned)ceil_div(nrows, R), ngrids);
     FG_K_CASE(1, 1)
     FG_K_CASE(2, 1)
@@ -302,5 +351,82 @@ int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int n
     return set_error(ERR_UNSUPPORTED, "fft2_k_r2c: no kernel for %d x %d", N1, N2);
 }
 #undef FG_K_CASE
+
+// ---- autotuner ---------------------------------------------------------------------
+// Launch shape -> time: two untimed launches, then the median of five timed
+// ones (CUDA events on s).  The FFT's arithmetic per row / column does not
+// depend on the shape, so every shape gives bit-identical results.
+static int time_shape(FftPlan *p, void *grid, cudaStream_t s, int which, int v, cudaEvent_t e0, cudaEvent_t e1,
+                      double *ms) {
+    const int Ng = p->Ng, nh = p->nh;
+    auto launch = [&]() -> int {
+        if (which == 0) return fft2_k_r2c(Ng, p->half.tw, p->rtw, grid, grid, 1, s, v);
+        const long es = which == 1 ? nh : (long)Ng * nh, bs = which == 1 ? (long)Ng * nh : nh;
+        return fft2_cols(Ng, p->axis.tw, grid, grid, 1, nh, es, bs, Ng, -1, s, v);
+    };
+    for (int r = 0; r < 2; ++r) FG_TRY(launch());
+    float t[5];
+    for (int r = 0; r < 5; ++r) {
+        FG_CUDA(cudaEventRecord(e0, s));
+        FG_TRY(launch());
+        FG_CUDA(cudaEventRecord(e1, s));
+        FG_CUDA(cudaEventSynchronize(e1));
+        FG_CUDA(cudaEventElapsedTime(&t[r], e0, e1));
+    }
+    for (int a = 1; a < 5; ++a)
+        for (int b = a; b > 0 && t[b] < t[b - 1]; --b) {
+            const float x = t[b];
+            t[b] = t[b - 1];
+            t[b - 1] = x;
+        }
+    *ms = t[2];
+    return OK;
+}
+
+int fft2_autotune(FftPlan *p, void *grid, cudaStream_t s, double ms[3]) {
+    if (!fft2_supported(p->Ng, p->prec))
+        return set_error(ERR_UNSUPPORTED, "autotune: no tunable launch shapes for Ng=%d (%s grid)", p->Ng,
+                         p->prec == 4 ? "FP32" : "FP64");
+    const size_t bytes = sizeof(float) * (size_t)p->Ng * p->Ng * 2 * p->nh;
+    FG_CUDA(cudaMemsetAsync(grid, 0, bytes, s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FG_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_check(ce, "autotune events");
+    }
+    int rc = OK;
+    int best[3];
+    double best_ms[3];
+    for (int which = 0; which < 3 && rc == OK; ++which) {
+        const int def = fft2_default_shape(p->Ng, which);
+        double def_ms = 0;
+        rc = time_shape(p, grid, s, which, def, e0, e1, &def_ms);
+        best[which] = def;
+        best_ms[which] = def_ms;
+        const int lo = which == 0 ? 1 : 0, hi = which == 0 ? 64 : 5;
+        for (int v = lo; v <= hi && rc == OK; v = which == 0 ? v * 2 : v + 1) {
+            if (v == def || !fft2_valid_shape(p->Ng, which, v)) continue;
+            double t = 0;
+            rc = time_shape(p, grid, s, which, v, e0, e1, &t);
+            // keep the built-in shape unless another is clearly faster (2 %)
+            if (rc == OK && t < best_ms[which] && t < 0.98 * def_ms) {
+                best[which] = v;
+                best_ms[which] = t;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == OK) rc = cuda_check(cudaMemsetAsync(grid, 0, bytes, s), "autotune clear");
+    if (rc == OK) rc = cuda_check(cudaStreamSynchronize(s), "autotune");
+    FG_TRY(rc);
+    p->tune[0] = best[0];
+    p->tune[1] = best[1];
+    p->tune[2] = best[2];
+    for (int w = 0; w < 3; ++w) ms[w] = best_ms[w];
+    return OK;
+}
 
 }  // namespace fg

@@ -18,6 +18,7 @@ enum Status {
     ERR_UNSUPPORTED = -4,
     ERR_RANGE = -5,
     ERR_STATE = -6,
+    ERR_IO = -7,
 };
 
 // records a status with a message (thread-local); returns the status
@@ -68,6 +69,10 @@ struct FftPlan {
     int cols = 16, col_threads = 256;      // column kernel: columns per CTA
     int rows = 16, row_threads = 256;      // k-axis kernel: rows per CTA
     size_t col_smem = 0, row_smem = 0;
+    // launch shapes of the two-level FP32 kernels (fft2.cu), set by the
+    // autotuner or a plan file: [0] k-pass rows per CTA (0 = built-in),
+    // [1] j-pass and [2] i-pass log2 columns per CTA (-1 = built-in)
+    int tune[3] = {0, -1, -1};
 };
 
 int fft_plan_create(FftPlan *p, int Ng, int prec);
@@ -83,8 +88,21 @@ int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaS
 // two-level FP32 kernels (fft2.cu) for power-of-two Ng in [4, 1024]
 bool fft2_supported(int Ng, int prec);
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
-              long nbatch, int sign, cudaStream_t s);
-int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s);
+              long nbatch, int sign, cudaStream_t s, int logC_req = -1);
+int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s,
+               int R_req = 0);
+// launch shape `v` of pass `which` (0 = k rows per CTA, 1 = j / 2 = i log2
+// columns per CTA) is launchable for Ng; the built-in choice of each pass
+bool fft2_valid_shape(int Ng, int which, int v);
+int fft2_default_shape(int Ng, int which);
+// time every valid launch shape of the three r2c passes on `grid` (one FP32
+// grid of the plan's size; its contents are transformed in place) and keep the
+// fastest in p->tune; ms[3] = the chosen shapes' times
+int fft2_autotune(FftPlan *p, void *grid, cudaStream_t s, double ms[3]);
+// plan cache (plan.cu): the entry of `path` for this device and the plan's
+// size, else the in-process cache, else fft2_autotune on `grid`; writes the
+// entry back to `path`.  *source: FFTGAL_PLAN_*; ms: measured times or 0.
+int plan_resolve(FftPlan *p, void *grid, cudaStream_t s, const char *path, bool quiet, int *source, double ms[3]);
 // i-axis pass of two grids fused with the interlacing finish:
 // A <- scale * 0.5 * (A + B * phaseB) * Winv3   (see spectral tables)
 int fft_pass_i_interlace(const FftPlan *p, void *gridA, void *gridB,

@@ -21,6 +21,7 @@ extern "C" {
 #define FFTGAL_ERR_UNSUPPORTED (-4)
 #define FFTGAL_ERR_RANGE (-5)
 #define FFTGAL_ERR_STATE (-6)
+#define FFTGAL_ERR_IO (-7)
 
 /* host-view modes of fft_t.f (see include/fft.h) */
 #define FFTGAL_VIEW_SYNC 0
@@ -155,6 +156,33 @@ int fftgal_alias_features(int NK, const double *K, const double *P, double Pshot
 /* e(u) = u^6 / (1 + u^6), u = k / k_Nyq: the scale of the perceptron's
  * outputs, P_l^interlaced - P_l^single = (|P0| + Pshot) e(u) y_l */
 double fftgal_alias_envelope(double u);
+/* Plan cache (the counterpart of FFTW wisdom, src/fft.c:26-45).  fft_init(Ng,
+ * L, path) with a file name instead of "FFTW_ESTIMATE" takes the launch shapes
+ * of the FP32 r2c passes (k-pass rows per CTA, j- and i-pass log2 columns per
+ * CTA) from the file's entry for this device (compute capability and SM count),
+ * Ng and precision; without one it measures every valid shape on the new grid
+ * (the FFTW_MEASURE step) and writes the entry back, keeping the file's other
+ * lines.  Shapes change no result: every shape computes each row and column
+ * with the same operations.  Grids whose FFT has no tunable shapes (FP64,
+ * Ng not a power of two in [4, 1024]) use the built-in plans. */
+#define FFTGAL_PLAN_BUILTIN 0  /* "FFTW_ESTIMATE", or nothing to tune */
+#define FFTGAL_PLAN_MEASURED 1 /* measured by this fft_init */
+#define FFTGAL_PLAN_FILE 2     /* imported from the plan file */
+#define FFTGAL_PLAN_CACHE 3    /* measured earlier in this process */
+/* the grid's shapes (tune[0] k rows, tune[1] j, tune[2] i log2 columns; 0 / -1
+ * = built-in), where they came from, and the measured times (ms, 0 unless
+ * measured) */
+int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms[3]);
+/* measure now (clears the grid) and keep the fastest shapes on this grid */
+int fftgal_plan_autotune(fft_t *grid, double ms[3]);
+/* host-only plan file access: 1 and tune[] if `path` holds an entry for the
+ * key, 0 if not (or no file); store replaces the key's entry */
+int fftgal_plan_lookup(const char *path, int cc, int sms, int Ng, int prec, int tune[3]);
+int fftgal_plan_store(const char *path, int cc, int sms, int Ng, int prec, const int tune[3],
+                      const double ms[3], const char *device_name);
+/* 1 if `shape` is launchable for pass 0 (k), 1 (j) or 2 (i) at Ng */
+int fftgal_plan_valid(int Ng, int pass, int shape);
+
 /* fftgal_power_single_f32 with P_0,2,4 corrected by the perceptron with host
  * parameters mlp_params (wedges and P_6 as measured): one paint and one FFT
  * instead of two of each. */

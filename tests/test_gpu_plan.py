@@ -1,0 +1,103 @@
+"""Autotuner and plan cache (csrc/plan.cu, fft2_autotune): fft_init with a
+plan file measures once, imports afterwards, reuses in-process measurements,
+re-measures an entry that does not fit, and every launch shape gives a
+k-space grid bit-identical to the built-in plans' (the counterpart of
+FFTW_MEASURE vs FFTW_ESTIMATE, src/fft.c:26-45)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+L_BOX = 1000.0
+
+
+@pytest.fixture(scope="module")
+def fg():
+    from fftgal_gb300 import build
+    build.build()
+    import fftgal_gb300
+    return fftgal_gb300
+
+
+def _kgrid(fg, Ng, wisdom, seed=3, Np=200000):
+    rng = np.random.default_rng(seed)
+    x, y, z = (rng.uniform(0, L_BOX, Np) for _ in range(3))
+    g = fg.Grid(Ng, L_BOX, wisdom=str(wisdom), precision="f32", host_view="sync")
+    cat = fg.Catalog(x, y, z, V=L_BOX ** 3)
+    g.p2k(cat)
+    return g, g.f.copy()
+
+
+def _entries(path):
+    return [l for l in path.read_text().splitlines() if l.startswith("fftgal_gb300-plan 1 ")]
+
+
+def test_measure_then_import(fg, tmp_path):
+    path = tmp_path / "plan"
+    g, f_tuned = _kgrid(fg, 64, path)
+    info = g.plan_info()
+    assert info["source"] == fg.PLAN_MEASURED
+    assert np.all(info["ms"] > 0)
+    lib = fg.lib()
+    for w in range(3):
+        assert lib.fftgal_plan_valid(64, w, info["tune"][w]) == 1
+    (line,) = _entries(path)
+    assert "Ng=64 prec=4" in line
+    g2, f_imported = _kgrid(fg, 64, path)
+    assert g2.plan_info()["source"] == fg.PLAN_FILE and g2.plan_info()["tune"] == info["tune"]
+    _, f_est = _kgrid(fg, 64, "FFTW_ESTIMATE")
+    np.testing.assert_array_equal(f_tuned, f_est)
+    np.testing.assert_array_equal(f_imported, f_est)
+    # a new file in the same process: the measurement is reused, then exported
+    path2 = tmp_path / "plan2"
+    g3, _ = _kgrid(fg, 64, path2)
+    assert g3.plan_info()["source"] == fg.PLAN_CACHE and g3.plan_info()["tune"] == info["tune"]
+    assert len(_entries(path2)) == 1
+
+
+@pytest.mark.parametrize("Ng", [128, 256])
+def test_every_valid_shape_is_bit_identical(fg, tmp_path, Ng):
+    """Entries with the smallest and the largest valid shape of every pass."""
+    lib = fg.lib()
+    _, f_est = _kgrid(fg, Ng, "FFTW_ESTIMATE")
+    ks = [r for r in (1, 2, 4, 8, 16, 32, 64) if lib.fftgal_plan_valid(Ng, 0, r)]
+    cs = {w: [c for c in range(6) if lib.fftgal_plan_valid(Ng, w, c)] for w in (1, 2)}
+    assert len(ks) >= 2 and len(cs[1]) >= 2 and len(cs[2]) >= 2
+    import torch
+    cc = "%d%d" % torch.cuda.get_device_capability()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for pick in (0, -1):
+        tune = [ks[pick], cs[1][pick], cs[2][pick]]
+        path = tmp_path / f"plan{pick}"
+        path.write_text(f"fftgal_gb300-plan 1 cc={cc} sms={sms} Ng={Ng} prec=4 kR={tune[0]} "
+                        f"jlogC={tune[1]} ilogC={tune[2]} ms=0,0,0 dev=hand written\n")
+        g, f = _kgrid(fg, Ng, path)
+        assert g.plan_info()["source"] == fg.PLAN_FILE and g.plan_info()["tune"] == tune
+        np.testing.assert_array_equal(f, f_est)
+
+
+def test_entry_that_does_not_fit_is_measured_again(fg, tmp_path):
+    import torch
+    cc = "%d%d" % torch.cuda.get_device_capability()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    path = tmp_path / "plan"
+    path.write_text(f"fftgal_gb300-plan 1 cc={cc} sms={sms} Ng=32 prec=4 kR=3 jlogC=9 ilogC=2 ms=0,0,0 dev=x\n")
+    g, f = _kgrid(fg, 32, path)
+    info = g.plan_info()
+    assert info["source"] in (fg.PLAN_MEASURED, fg.PLAN_CACHE)
+    lib = fg.lib()
+    for w in range(3):
+        assert lib.fftgal_plan_valid(32, w, info["tune"][w]) == 1
+    (line,) = _entries(path)
+    assert "kR=3 " not in line
+    _, f_est = _kgrid(fg, 32, "FFTW_ESTIMATE")
+    np.testing.assert_array_equal(f, f_est)
+
+
+def test_fp64_and_untunable_sizes_use_builtin_plans(fg, tmp_path):
+    path = tmp_path / "plan"
+    g = fg.Grid(48, L_BOX, wisdom=str(path), precision="f32")
+    assert g.plan_info()["source"] == fg.PLAN_BUILTIN
+    g = fg.Grid(64, L_BOX, wisdom=str(path), precision="f64")
+    assert g.plan_info()["source"] == fg.PLAN_BUILTIN
+    assert not path.exists()
