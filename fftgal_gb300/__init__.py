@@ -112,6 +112,7 @@ SIGNATURES = {
     "fftgal_plan_store": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), _dp,
                                     C.c_char_p]),
     "fftgal_plan_valid": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+    "fftgal_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "fftgal_power_learned_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                            C.c_int, _dp, C.c_double, C.c_int, C.POINTER(C.c_float), _dp, _lp,
                                            _dp, _dp, _lp, _dp]),
@@ -314,6 +315,10 @@ class Grid:
 
     def sync_device(self):
         _check(lib().fftgal_sync_device(self.p))
+
+    def set_graphs(self, on: bool):
+        """Graph-captured batches on (default) or off (fftgal_set_graphs)."""
+        _check(lib().fftgal_set_graphs(self.p, int(bool(on))))
 
     def plan_info(self) -> dict:
         """Launch shapes of the FFT passes (fftgal_plan_info): ``tune`` = [k rows

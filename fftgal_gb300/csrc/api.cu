@@ -114,6 +114,19 @@ struct Grid {
     double stage_ms[kStages + 1] = {};
     int plan_source = FFTGAL_PLAN_BUILTIN;
     double plan_ms[3] = {0, 0, 0};
+    // graph-captured batches: one executable graph per upload buffer, the
+    // per-catalog scalars it reads (device, one block per buffer; pinned
+    // host ring, one block per catalog) and a pinned ring of bin sums
+    int use_graphs = 1;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    std::vector<uint64_t> gkey;  // everything the captured graphs depend on
+    int graph_kernels = 0;       // kernel nodes per graph
+    DevScalars *d_scal = nullptr;
+    DevScalars *h_scal = nullptr;
+    size_t h_scal_cap = 0;
+    double *h_acc = nullptr;
+    size_t h_acc_cap = 0;
 };
 
 static Grid *G(const fft_t *f) { return f ? reinterpret_cast<Grid *>(f->x2k) : nullptr; }
@@ -128,6 +141,11 @@ static int env_precision() {
 static int env_view() {
     const char *e = getenv("FFTGAL_HOST_VIEW");
     return (e && !strcmp(e, "lazy")) ? FFTGAL_VIEW_LAZY : FFTGAL_VIEW_SYNC;
+}
+
+static int env_graphs() {
+    const char *e = getenv("FFTGAL_GRAPHS");
+    return !(e && !strcmp(e, "0"));
 }
 
 static int env_quiet() {
@@ -375,6 +393,7 @@ extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
     g->prec = env_precision();
     g->view = env_view();
     g->quiet = env_quiet();
+    g->use_graphs = env_graphs();
     g->Ng = Ng;
     g->Ng_pad = self->Ng_pad;
     g->nh = Ng / 2 + 1;
@@ -423,6 +442,12 @@ extern "C" void fft_free(fft_t *self) {
                 if (g->buf_free[b]) cudaEventDestroy(g->buf_free[b]);
             }
             if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
+            for (int b = 0; b < 2; ++b)
+                if (g->gexec[b]) cudaGraphExecDestroy(g->gexec[b]);
+            if (g->cap_stream) cudaStreamDestroy(g->cap_stream);
+            cudaFree(g->d_scal);
+            if (g->h_scal) cudaFreeHost(g->h_scal);
+            if (g->h_acc) cudaFreeHost(g->h_acc);
             cudaFree(g->d_stage);
             cudaFree(g->d_tab);
             fft_plan_destroy(&g->fft);
@@ -1134,6 +1159,216 @@ extern "C" int fftgal_dl_sub(fft_t *grid, int sphere, int Nsub, int nlos, const 
     return leave(grid, true);
 }
 
+// ---- graph-captured batches ------------------------------------------------------
+// The device work of one catalog -- paint key, scan, scatter and tile paint of
+// both interlacing grids, the three r2c passes, the fused finish + binning --
+// is captured once per upload buffer into a CUDA graph whose kernels read the
+// catalog's count and scales from a device block (DevScalars), so one graph
+// replays for catalogs of any size.  The host enqueues upload, graph and the
+// read-back of the bin sums for every catalog without waiting, and finishes
+// all bin tables after one synchronisation.
+static void graphs_drop(Grid *g) {
+    for (int b = 0; b < 2; ++b)
+        if (g->gexec[b]) {
+            cudaGraphExecDestroy(g->gexec[b]);
+            g->gexec[b] = nullptr;
+        }
+    g->gkey.clear();
+}
+
+static int enqueue_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cudaStream_t st) {
+    Grid *g = G(grid);
+    const float *d = g->d_batch[b];
+    const int Ng = grid->Ng;
+    PaintGridSpec spec[2];
+    spec[0].out = g->d_f;
+    spec[1].out = g->d_aux;
+    for (int a = 0; a < 3; ++a) {
+        spec[0].offset[a] = 0;
+        spec[1].offset[a] = remainder(0.5, Ng);
+    }
+    FG_TRY(paint(&g->tiling, &g->scratch, 4, d, d + capNp, d + 2 * capNp, 4, capNp, Ng / grid->L, spec, 2, st,
+                 nullptr, nullptr, g->d_scal + b));
+    void *grids[2] = {g->d_f, g->d_aux};
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
+    FG_TRY(fft_pass_j(&g->fft, grids, 2, -1, st));
+    FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
+    BinFinish fin;
+    fin.A = g->d_f;
+    fin.B = g->d_aux;
+    fin.ph32 = dual_tab32(g);
+    fin.w32 = winv_tab32(g);
+    fin.scale = 0.5 * H3_of(g);
+    return bin_power_launch(geo, 2, 0, 0, st, &fin, g->d_scal + b);
+}
+
+static int capture_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cudaGraphExec_t *exec, int *nkern) {
+    Grid *g = G(grid);
+    cudaStream_t cs = g->cap_stream;
+    FG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+    const int rc = enqueue_catalog(grid, b, capNp, geo, cs);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    if (rc != OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return rc != OK ? rc : cuda_check(e, "graph capture");
+    }
+    size_t n = 0;
+    e = cudaGraphGetNodes(graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (e == cudaSuccess && n) e = cudaGraphGetNodes(graph, nodes.data(), &n);
+    int k = 0;
+    for (size_t q = 0; q < n && e == cudaSuccess; ++q) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[q], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    *nkern = k;
+    return cuda_check(e, "graph instantiate");
+}
+
+template <typename T>
+static void key_push(std::vector<uint64_t> &k, T v) {
+    uint64_t u = 0;
+    memcpy(&u, &v, sizeof(T) < sizeof(u) ? sizeof(T) : sizeof(u));
+    k.push_back(u);
+}
+
+static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const float *const *y,
+                             const float *const *z, const long *Np, const double *V, const double los_in[3],
+                             double dK, int Nmu, double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
+                             double *Pmu) {
+    Grid *g = G(grid);
+    long maxNp = 0;
+    for (int c = 0; c < ncat; ++c) {
+        if (!x[c] || !y[c] || !z[c] || Np[c] <= 0 || !(V[c] > 0))
+            return set_error(ERR_ARG, "fftgal_power_batch_f32: bad catalog %d", c);
+        maxNp = Np[c] > maxNp ? Np[c] : maxNp;
+    }
+    if (ncat == 0) return OK;
+    if (!g->copy_stream) FG_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    if (!g->cap_stream) FG_CUDA(cudaStreamCreateWithFlags(&g->cap_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        if (!g->up_done[b]) FG_CUDA(cudaEventCreateWithFlags(&g->up_done[b], cudaEventDisableTiming));
+        if (!g->buf_free[b]) FG_CUDA(cudaEventCreateWithFlags(&g->buf_free[b], cudaEventDisableTiming));
+    }
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    FG_CUDA(cudaStreamSynchronize(g->copy_stream));
+    if ((size_t)3 * maxNp > g->batch_cap) {
+        graphs_drop(g);
+        for (int b = 0; b < 2; ++b) {
+            cudaFree(g->d_batch[b]);
+            g->d_batch[b] = nullptr;
+        }
+        g->batch_cap = 0;
+        for (int b = 0; b < 2; ++b) FG_CUDA(cudaMalloc(&g->d_batch[b], sizeof(float) * 3 * maxNp));
+        g->batch_cap = (size_t)3 * maxNp;
+    }
+    const long capNp = (long)(g->batch_cap / 3);
+    FG_TRY(ensure_aux(g));
+    FG_TRY(ensure_tables(g));
+    FG_TRY(fft2_prepare());
+    FG_TRY(paint_reserve(&g->tiling, &g->scratch, capNp));
+    if (!g->d_scal) FG_CUDA(cudaMalloc(&g->d_scal, 2 * sizeof(DevScalars)));
+    double los[3] = {los_in[0], los_in[1], los_in[2]};
+    hat(los);
+    BinSpec spec;
+    FG_TRY(bin_spec_init(&spec, grid->Ng, grid->L, dK, los, Nmu));
+    BinGeometry *geo = geometry(g, spec);
+    if (!geo) return t_status ? t_status : ERR_CUDA;
+    if (geo->bad)
+        return set_error(ERR_RANGE, "a mode falls beyond the last of NK=%d k bins (dK too small for Ng)", spec.NK);
+    if ((size_t)ncat > g->h_scal_cap) {
+        if (g->h_scal) cudaFreeHost(g->h_scal);
+        g->h_scal = nullptr;
+        g->h_scal_cap = 0;
+        FG_CUDA(cudaMallocHost(&g->h_scal, sizeof(DevScalars) * ncat));
+        g->h_scal_cap = ncat;
+    }
+    if ((size_t)ncat * geo->acc_len > g->h_acc_cap) {
+        if (g->h_acc) cudaFreeHost(g->h_acc);
+        g->h_acc = nullptr;
+        g->h_acc_cap = 0;
+        FG_CUDA(cudaMallocHost(&g->h_acc, sizeof(double) * ncat * geo->acc_len));
+        g->h_acc_cap = (size_t)ncat * geo->acc_len;
+    }
+    // recapture whenever a buffer, table, plan or bin layout the graphs name changed
+    std::vector<uint64_t> key;
+    const void *ptrs[] = {g->d_batch[0], g->d_batch[1], g->d_f,         g->d_aux,           g->scratch.key,
+                          g->scratch.rank, g->scratch.sorted, g->scratch.hist, g->scratch.scan_tmp, geo,
+                          geo->d_acc,      geo->d_thr,        g->d_tab,       g->d_scal};
+    for (const void *q : ptrs) key_push(key, (uintptr_t)q);
+    key_push(key, capNp);
+    for (int w = 0; w < 3; ++w) key_push(key, g->fft.tune[w]);
+    key_push(key, spec.NK);
+    key_push(key, Nmu);
+    key_push(key, dK);
+    for (int a = 0; a < 3; ++a) key_push(key, los[a]);
+    if (key != g->gkey) {
+        graphs_drop(g);
+        for (int b = 0; b < 2; ++b) FG_TRY(capture_catalog(grid, b, capNp, geo, &g->gexec[b], &g->graph_kernels));
+        g->gkey = key;
+    }
+    // per-catalog scalars, formed like power_f32_run forms its launch arguments
+    const double H3 = H3_of(g);
+    for (int c = 0; c < ncat; ++c) {
+        DevScalars &q = g->h_scal[c];
+        const double nbar = Np[c] / V[c];
+        q.Np = Np[c];
+        q.scale[0] = q.scale[1] = 1 / nbar / H3;
+        q.Vinv = (float)(1 / V[c]);
+        q.Pshot = (float)(V[c] / Np[c]);
+    }
+    auto upload = [&](int c) -> int {
+        const int b = c & 1;
+        float *d = g->d_batch[b];
+        FG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->buf_free[b], 0));
+        const float *src[3] = {x[c], y[c], z[c]};
+        for (int a = 0; a < 3; ++a)
+            FG_CUDA(cudaMemcpyAsync(d + (size_t)a * capNp, src[a], sizeof(float) * Np[c], cudaMemcpyHostToDevice,
+                                    g->copy_stream));
+        FG_CUDA(cudaMemcpyAsync(g->d_scal + b, g->h_scal + c, sizeof(DevScalars), cudaMemcpyHostToDevice,
+                                g->copy_stream));
+        FG_CUDA(cudaEventRecord(g->up_done[b], g->copy_stream));
+        return OK;
+    };
+    for (int b = 0; b < 2; ++b) FG_CUDA(cudaEventRecord(g->buf_free[b], g->stream));
+    FG_TRY(upload(0));
+    for (int c = 0; c < ncat; ++c) {
+        const int b = c & 1;
+        if (c + 1 < ncat) FG_TRY(upload(c + 1));
+        FG_CUDA(cudaStreamWaitEvent(g->stream, g->up_done[b], 0));
+        FG_CUDA(cudaGraphLaunch(g->gexec[b], g->stream));
+        note_launches(g->graph_kernels);
+        FG_CUDA(cudaEventRecord(g->buf_free[b], g->stream));
+        FG_CUDA(cudaMemcpyAsync(g->h_acc + (size_t)c * geo->acc_len, geo->d_acc, sizeof(double) * geo->acc_len,
+                                cudaMemcpyDeviceToHost, g->stream));
+    }
+    FG_CUDA(cudaStreamSynchronize(g->stream));
+    FG_CUDA(cudaStreamSynchronize(g->copy_stream));
+    for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
+    ++g->version;
+    const int NK = spec.NK;
+    std::vector<double> Psum((size_t)NK * 4), Pw((size_t)NK * (Nmu + 1));
+    for (int c = 0; c < ncat; ++c) {
+        bin_power_unpack(geo, g->h_acc + (size_t)c * geo->acc_len, Psum.data(), Pw.data());
+        const size_t o1 = (size_t)NK * c, o4 = (size_t)NK * 4 * c, om = (size_t)NK * Nmu * c;
+        FG_TRY(finish_pl(geo, Psum, K ? K + o1 : nullptr, N ? N + o1 : nullptr, Pl ? Pl + o4 : nullptr));
+        FG_TRY(finish_pmu(geo, Pw, Kmu ? Kmu + om : nullptr, Nmu_count ? Nmu_count + om : nullptr,
+                          Pmu ? Pmu + om : nullptr));
+    }
+    if (g->view == FFTGAL_VIEW_SYNC) FG_TRY(device_to_host(g, grid->f, g->pinned));
+    return OK;
+}
+
+extern "C" int fftgal_set_graphs(fft_t *grid, int on) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    G(grid)->use_graphs = on ? 1 : 0;
+    return OK;
+}
+
 extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const float *const *y,
                                       const float *const *z, const long *Np, const double *V,
                                       const double los[3], double dK, int Nmu, double *K, long *N, double *Pl,
@@ -1142,6 +1377,8 @@ extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const 
         return set_error(ERR_ARG, "fftgal_power_batch_f32: bad arguments");
     Grid *g = G(grid);
     if (g->prec != 4) return set_error(ERR_STATE, "fftgal_power_batch_f32 needs an FP32 grid");
+    if (g->use_graphs)
+        return power_batch_graph(grid, ncat, x, y, z, Np, V, los, dK, Nmu, K, N, Pl, Kmu, Nmu_count, Pmu);
     long maxNp = 0;
     for (int c = 0; c < ncat; ++c) {
         if (!x[c] || !y[c] || !z[c] || Np[c] <= 0 || !(V[c] > 0))

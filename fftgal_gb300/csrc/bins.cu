@@ -315,7 +315,11 @@ struct SlabFinish {
 template <int MODE>
 __global__ void __launch_bounds__(kSlabThreads, 3)
 bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, float Vinv, float Pshot,
-                      const uint32_t *__restrict__ thr_g, double *__restrict__ gacc) {
+                      const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, const DevScalars *__restrict__ ds) {
+    if (ds) {
+        Vinv = ds->Vinv;
+        Pshot = ds->Pshot;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int NK = d.NK, W = d.W, NQ = 4 + W;
     float *acc32 = reinterpret_cast<float *>(smem_raw);                        // [NQ][NK]
@@ -418,8 +422,36 @@ static size_t slab_smem(int NK, int NQ) {
            sizeof(float) * (kSlabThreads / 32) * kSlabJ * kSlabRow;
 }
 
+static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot, cudaStream_t st,
+                      const BinFinish *fin, const DevScalars *ds);
+
+void bin_power_unpack(const BinGeometry *g, const double *h, double *Psum, double *Pw) {
+    const int NK = g->spec.NK, W = g->spec.Nmu + 1, NQ = 4 + W;
+    for (int b = 0; b < NK; ++b) {
+        for (int l = 0; l < 4; ++l) Psum[b * 4 + l] = h[(size_t)b * NQ + l];
+        for (int m = 0; m < W; ++m) Pw[(size_t)b * W + m] = h[(size_t)b * NQ + 4 + m];
+    }
+}
+
+int bin_power_launch(BinGeometry *g, int mode, double Vinv, double Pshot, cudaStream_t st, const BinFinish *fin,
+                     const DevScalars *ds) {
+    if (mode < 2) return set_error(ERR_ARG, "bin_power_launch: modes 2 and 3 only");
+    return bin_launch(g, nullptr, 4, mode, Vinv, Pshot, st, fin, ds);
+}
+
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
               double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end, const BinFinish *fin) {
+    FG_TRY(bin_launch(g, f, prec, mode, Vinv, Pshot, st, fin, nullptr));
+    if (ev_end) FG_CUDA(cudaEventRecord(*ev_end, st));
+    std::vector<double> h(g->acc_len);
+    FG_CUDA(cudaMemcpyAsync(h.data(), g->d_acc, sizeof(double) * g->acc_len, cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    bin_power_unpack(g, h.data(), Psum, Pw);
+    return OK;
+}
+
+static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot, cudaStream_t st,
+                      const BinFinish *fin, const DevScalars *ds) {
     if (!g->valid) return set_error(ERR_STATE, "bin geometry not built");
     if (mode >= 2 && (prec != 4 || !fin)) return set_error(ERR_ARG, "fused finish needs an FP32 grid");
     const BinSpec &s = g->spec;
@@ -449,7 +481,7 @@ int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, do
         FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                                      (int)smem));                                                           \
         bin_power_slab_kernel<M><<<(unsigned)nb, kSlabThreads, smem, st>>>(d, fv, sf, (float)Vinv, (float)Pshot, \
-                                                                         g->d_thr, g->d_acc);               \
+                                                                         g->d_thr, g->d_acc, ds);           \
     } while (0)
         if (mode == 0)
             FG_SLAB_LAUNCH(0);
@@ -481,14 +513,6 @@ int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, do
 #undef FG_BIN_LAUNCH
     }
     FG_LAUNCHED(1);
-    if (ev_end) FG_CUDA(cudaEventRecord(*ev_end, st));
-    std::vector<double> h(g->acc_len);
-    FG_CUDA(cudaMemcpyAsync(h.data(), g->d_acc, sizeof(double) * g->acc_len, cudaMemcpyDeviceToHost, st));
-    FG_CUDA(cudaStreamSynchronize(st));
-    for (int b = 0; b < NK; ++b) {
-        for (int l = 0; l < 4; ++l) Psum[b * 4 + l] = h[(size_t)b * NQ + l];
-        for (int m = 0; m < W; ++m) Pw[(size_t)b * W + m] = h[(size_t)b * NQ + 4 + m];
-    }
     return OK;
 }
 

@@ -279,6 +279,8 @@ int fft2_default_shape(int Ng, int which) {
     return cols_default_logC(N2, es * (long)sizeof(float2) > (1L << 20));
 }
 
+int fft2_prepare() { return ensure_w32(); }
+
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
               long nbatch, int sign, cudaStream_t s, int logC_req) {
     FG_TRY(ensure_w32());

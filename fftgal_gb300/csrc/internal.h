@@ -95,6 +95,8 @@ int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int n
 // columns per CTA) is launchable for Ng; the built-in choice of each pass
 bool fft2_valid_shape(int Ng, int which, int v);
 int fft2_default_shape(int Ng, int which);
+// device twiddle tables of the two-level kernels (built once per device)
+int fft2_prepare();
 // time every valid launch shape of the three r2c passes on `grid` (one FP32
 // grid of the plan's size; its contents are transformed in place) and keep the
 // fastest in p->tune; ms[3] = the chosen shapes' times
@@ -149,14 +151,27 @@ struct PaintRsd {
     double aHinv = 0;
 };
 
+// Per-catalog scalars that the kernels read from device memory instead of
+// their launch arguments, so that one captured CUDA graph serves catalogs of
+// any size (graph-captured batches): the particle count, the paint scales of
+// the two grids, and the binning's 1/V and shot noise.
+struct DevScalars {
+    long Np;
+    double scale[2];
+    float Vinv, Pshot;
+};
+
 // Paint one catalog onto 1 or 2 grids (same tiling, offsets within 1 cell of
 // each other).  pos_prec: 4 (float x,y,z) or 8 (double x,y,z); device pointers.
 // `ev` (optional, 4 events) is recorded after the key, scan, scatter and
-// tile-paint kernels.
+// tile-paint kernels.  With `ds` (device, FP32 only) the kernels take Np and
+// the grids' scales from *ds; Np is then the capacity (the largest count).
 int paint(const PaintTiling *t, PaintScratch *s, int grid_prec,
           const void *x, const void *y, const void *z, int pos_prec, long Np,
           double Hinv, const PaintGridSpec *grids, int ngrids, cudaStream_t st,
-          cudaEvent_t *ev = nullptr, const PaintRsd *rsd = nullptr);
+          cudaEvent_t *ev = nullptr, const PaintRsd *rsd = nullptr, const DevScalars *ds = nullptr);
+// scratch for catalogs of up to Np particles (no allocation in later paints)
+int paint_reserve(const PaintTiling *t, PaintScratch *s, long Np);
 
 // ---- spectral elementwise ----------------------------------------------------
 int scale_grid(void *f, long n, int prec, double s, cudaStream_t st);
@@ -225,6 +240,13 @@ struct BinFinish {
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
               double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end = nullptr,
               const BinFinish *fin = nullptr);
+// the launches of bin_power (FP32, modes 2 and 3) without the read-back: the
+// sums stay in g->d_acc ([NK][4 + Nmu + 1] doubles); with `ds` the kernel
+// takes Vinv and Pshot from device memory
+int bin_power_launch(BinGeometry *g, int mode, double Vinv, double Pshot, cudaStream_t st, const BinFinish *fin,
+                     const DevScalars *ds);
+// Psum / Pw of bin_power from a copy of g->d_acc
+void bin_power_unpack(const BinGeometry *g, const double *acc, double *Psum, double *Pw);
 
 // ---- misc -----------------------------------------------------------------------
 int num_sms();

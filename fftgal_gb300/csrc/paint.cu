@@ -245,7 +245,8 @@ template <typename P>
 __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ y,
                                  const P *__restrict__ z, long Np, PaintParams pp,
                                  uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
-                                 uint32_t *__restrict__ hist) {
+                                 uint32_t *__restrict__ hist, const DevScalars *__restrict__ ds) {
+    if (ds) Np = ds->Np;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
         P pos[3] = {x[p], y[p], z[p]};
         rsd_displace(pp, p, pos);
@@ -351,7 +352,9 @@ __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restric
                                      const uint32_t *__restrict__ key,
                                      const uint32_t *__restrict__ rank,
                                      const uint32_t *__restrict__ off,
-                                     typename Rec<P>::type *__restrict__ sorted) {
+                                     typename Rec<P>::type *__restrict__ sorted,
+                                     const DevScalars *__restrict__ ds) {
+    if (ds) Np = ds->Np;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
         const uint32_t dst = off[key[p]] + rank[p];
         typename Rec<P>::type r;
@@ -386,6 +389,7 @@ struct PaintOut {
     void *out[kMaxPaintGrids];
     double scale[kMaxPaintGrids];
     int accumulate[kMaxPaintGrids];
+    const DevScalars *ds;  // if set, the scales are ds->scale
 };
 
 // Tile geometry and the flattened list of particle segments a tile pulls:
@@ -829,8 +833,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             const int te1 = ts.te[1], te2 = ts.te[2];
             const long rstride = (long)pp.Ng_pad;  // global floats between consecutive j
             const long istride = rstride * Ng;     // and between consecutive i
-            const float sc0 = (float)ldexp(po.scale[0], fixed ? -fixbits : 0);
-            const float sc1 = ngr > 1 ? (float)ldexp(po.scale[1], fixed ? -fixbits : 0) : 0.f;
+            const double s0 = po.ds ? po.ds->scale[0] : po.scale[0], s1 = po.ds ? po.ds->scale[1] : po.scale[1];
+            const float sc0 = (float)ldexp(s0, fixed ? -fixbits : 0);
+            const float sc1 = ngr > 1 ? (float)ldexp(s1, fixed ? -fixbits : 0) : 0.f;
             const long obase = ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
             for (int li = warp; li < ts.te[0]; li += nwarp) {
                 float *o0 = reinterpret_cast<float *>(po.out[0]) + obase + li * istride;
@@ -1010,6 +1015,10 @@ static int ensure_scratch(PaintScratch *s, long Np, long nkeys) {
     return OK;
 }
 
+int paint_reserve(const PaintTiling *t, PaintScratch *s, long Np) {
+    return ensure_scratch(s, Np > 0 ? Np : 1, t->nkeys);
+}
+
 static void split(double v, float &hi, float &lo) {
     hi = (float)v;
     lo = (float)(v - (double)hi);
@@ -1017,8 +1026,9 @@ static void split(double v, float &hi, float &lo) {
 
 int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, const void *y, const void *z,
           int pos_prec, long Np, double Hinv, const PaintGridSpec *grids, int ngrids, cudaStream_t st,
-          cudaEvent_t *ev, const PaintRsd *rsd) {
+          cudaEvent_t *ev, const PaintRsd *rsd, const DevScalars *ds) {
     if (ngrids < 1 || ngrids > kMaxPaintGrids) return set_error(ERR_ARG, "paint: 1 or 2 grids");
+    if (ds && (grid_prec != 4 || pos_prec != 4)) return set_error(ERR_ARG, "paint: device scalars need FP32");
     if (rsd && rsd->v[0] && pos_prec != 4) return set_error(ERR_ARG, "paint: displacement needs FP32 positions");
     if (pos_prec != grid_prec) return set_error(ERR_ARG, "paint: position precision must match grid precision");
     if (Np < 0 || Np >= (1L << 32)) return set_error(ERR_ARG, "paint: Np out of range");
@@ -1069,6 +1079,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
         po.scale[g] = grids[g].scale;
         po.accumulate[g] = grids[g].accumulate;
     }
+    po.ds = ds;
     FG_TRY(ensure_scratch(s, Np > 0 ? Np : 1, t->nkeys));
     FG_CUDA(cudaMemsetAsync(s->hist, 0, sizeof(uint32_t) * (t->nkeys + 1), st));
     const int nsm = num_sms();
@@ -1076,10 +1087,10 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (Np > 0) {
         if (pos_prec == 4)
             paint_key_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z, Np,
-                                                       pp, s->key, s->rank, s->hist);
+                                                       pp, s->key, s->rank, s->hist, ds);
         else
             paint_key_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y, (const double *)z,
-                                                        Np, pp, s->key, s->rank, s->hist);
+                                                        Np, pp, s->key, s->rank, s->hist, nullptr);
         FG_LAUNCHED(1);
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[0], st));
@@ -1088,11 +1099,12 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (Np > 0) {
         if (pos_prec == 4)
             paint_scatter_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z,
-                                                           Np, pp, s->key, s->rank, s->hist, (uint4 *)s->sorted);
+                                                           Np, pp, s->key, s->rank, s->hist, (uint4 *)s->sorted,
+                                                           ds);
         else
             paint_scatter_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y,
                                                             (const double *)z, Np, pp, s->key, s->rank, s->hist,
-                                                            (Rec<double>::type *)s->sorted);
+                                                            (Rec<double>::type *)s->sorted, nullptr);
         FG_LAUNCHED(1);
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));

@@ -117,7 +117,14 @@ int fftgal_dl_sub(fft_t *grid, int sphere, int Nsub, int nlos, const double *los
  * behind the computation.  Outputs are the fftgal_power_f32 outputs of each
  * catalog one after another: K[ncat*NK], N[ncat*NK], Pl[ncat*NK*4],
  * Kmu/Nmu_count/Pmu[ncat*NK*Nmu] (any may be NULL).  Holds two device buffers
- * of 3 * max(Np) floats until fft_free. */
+ * of 3 * max(Np) floats until fft_free.
+ * By default (FFTGAL_GRAPHS unset or not "0", or fftgal_set_graphs(grid, 1))
+ * each catalog's device work runs as one CUDA graph launch: the sequence is
+ * captured once per upload buffer (again when the largest Np, the bins or a
+ * buffer change) with the kernels reading each catalog's count and scales
+ * from device memory; the host waits once per batch, not once per catalog.
+ * Per-stage timers (fftgal_stage_times) are not recorded in that mode. */
+int fftgal_set_graphs(fft_t *grid, int on);
 int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const float *const *y,
                            const float *const *z, const long *Np, const double *V,
                            const double los[3], double dK, int Nmu, double *K, long *N,

@@ -320,25 +320,56 @@ def test_fft_large_matches_cufft(fg, Ng):
     assert back_l2 <= 1e-6 and back_max <= 1e-5, (back_l2, back_max)
 
 
-def test_batch_matches_single_calls(fg):
-    """fftgal_power_batch_f32 (uploads on a second stream, two buffers) gives
-    each catalog's fftgal_power_f32 result: counts exact, P to 1e-6 of
-    (|P_0| + Pshot) (binning sums FP32 run totals in FP64 in a varying order)."""
-    Ng, L, Nmu = 64, 500.0, 4
-    los, dK = (0.0, 0.6, 0.8), 2 * np.pi / L
-    cats = [uniform_box(20 + c, n, L) for c, n in enumerate((40_000, 90_000, 25_000, 60_000, 5_000))]
-    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
-    got = g.power_batch_f32(cats, L ** 3, los, dK, Nmu=Nmu)
+def _check_batch(fg, g, got, cats, V, los, dK, Nmu):
     for c, cat in enumerate(cats):
-        want = g.power_f32(*cat, L ** 3, los, dK, Nmu=Nmu)
+        want = g.power_f32(*cat, V[c], los, dK, Nmu=Nmu)
         np.testing.assert_array_equal(got[c]["N"], want["N"])
         np.testing.assert_array_equal(got[c]["Nmu"], want["Nmu"])
-        den = np.abs(np.nan_to_num(want["P"][:, :1])) + L ** 3 / len(cat[0])
+        den = np.abs(np.nan_to_num(want["P"][:, :1])) + V[c] / len(cat[0])
         ok = np.isfinite(want["P"])
         err = (np.abs(got[c]["P"] - want["P"]) / den)[ok]
         assert err.max() <= 1e-6, f"catalog {c}: {err.max():.2e}"
         errw = np.abs(got[c]["Pmu"] - want["Pmu"]) / den
         assert errw.max() <= 1e-6, f"catalog {c} wedges: {errw.max():.2e}"
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_batch_matches_single_calls(fg, graphs):
+    """fftgal_power_batch_f32 (uploads on a second stream, two buffers; with
+    graphs, one CUDA graph launch per catalog) gives each catalog's
+    fftgal_power_f32 result: counts exact, P to 1e-6 of (|P_0| + Pshot)
+    (binning sums FP32 run totals in FP64 in a varying order)."""
+    Ng, L, Nmu = 64, 500.0, 4
+    los, dK = (0.0, 0.6, 0.8), 2 * np.pi / L
+    cats = [uniform_box(20 + c, n, L) for c, n in enumerate((40_000, 90_000, 25_000, 60_000, 5_000))]
+    V = [L ** 3 * f for f in (1.0, 0.5, 2.0, 1.0, 3.0)]
+    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
+    g.set_graphs(graphs)
+    got = g.power_batch_f32(cats, V, los, dK, Nmu=Nmu)
+    _check_batch(fg, g, got, cats, V, los, dK, Nmu)
+
+
+def test_graph_batches_recapture_and_reuse(fg):
+    """Graph batches on one grid across calls: the same captured graphs for
+    smaller catalogs, recapture for a larger catalog, other bins or another
+    line of sight; a batch of one catalog; the sync host view refreshed with
+    the last catalog's finished field as fftgal_power_f32 leaves it."""
+    Ng, L = 32, 300.0
+    dK = 2 * np.pi / L
+    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
+    calls = [((0, 0, 1), 3, (30_000, 20_000, 10_000)), ((0, 0, 1), 3, (5_000, 25_000)),
+             ((0, 0, 1), 3, (70_000, 1_000, 50_000)), ((1, 1, 0), 10, (20_000,)), ((0, 0, 1), 4, (8_000, 9_000))]
+    for q, (los, Nmu, sizes) in enumerate(calls):
+        cats = [uniform_box(100 * q + c, n, L) for c, n in enumerate(sizes)]
+        V = [L ** 3] * len(cats)
+        got = g.power_batch_f32(cats, V, los, dK, Nmu=Nmu)
+        _check_batch(fg, g, got, cats, V, los, dK, Nmu)
+    gs = fg.Grid(Ng, L, precision="f32", host_view="sync")
+    cats = [uniform_box(7, 12_000, L), uniform_box(8, 15_000, L)]
+    gs.power_batch_f32(cats, L ** 3, (0, 0, 1), dK)
+    f_batch = np.array(gs.f)
+    gs.power_f32(*cats[1], L ** 3, (0, 0, 1), dK)
+    np.testing.assert_allclose(f_batch, np.array(gs.f), rtol=0, atol=0)
 
 
 @pytest.mark.parametrize("prec,Ng,Nsub", [("f64", 16, 2), ("f64", 24, 3), ("f64", 32, 4), ("f32", 16, 2),
