@@ -509,11 +509,14 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, ui
     return r;
 }
 
-// deposit staged particles: lane = (grid, i row, j row), every lane adds its
-// row's 4 k cells.  By the bank layout each of the 4 atomic steps is a single
-// shared-memory wavefront.  Two particles are read before either is deposited
-// so the shared loads of one overlap the atomics of the other.  Stencil cells
-// outside the tile (local index kOut) are skipped.
+// deposit staged particles: lane = (grid, i row, j row), or (particle parity,
+// i row, j row) when one grid is painted; every lane adds its row's 4 k
+// cells.  By the bank layout each of the 4 atomic steps is a single
+// shared-memory wavefront (two grids).  The loop is unrolled so that the
+// shared loads of the next particles overlap the atomics of the current one
+// (unrolled by 4: 2 % faster than by 2 at Ng = 1024; one grid with the half
+// warps on alternate particles: 9.5 ms against 11.7 ms with one half idle).
+// Stencil cells outside the tile (local index kOut) are skipped.
 // slot of particle p of grid g in the stage buffer: the two grids' records
 // interleave so that lanes reading both fall in different banks
 __device__ __forceinline__ int stage_slot(int p, int g) { return 2 * p + g; }
@@ -566,11 +569,16 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
 
 template <bool FIXED, bool FAST>
 __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, int np, int ngr, int lane) {
-    const int g = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
-    if (g >= ngr) return;
+    const int h = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
     const int lane_off = a * kSI + b * kSJ;
+    if (ngr > 1) {
+#pragma unroll 4
+        for (int p = 0; p < np; ++p) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
+    } else {
+        // one grid: the half warps deposit alternate particles
 #pragma unroll 2
-    for (int p = 0; p < np; ++p) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, g), g, a, b, lane_off);
+        for (int p = h; p < np; p += 2) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, 0), 0, a, b, lane_off);
+    }
 }
 
 // largest fixed-point exponent s for which `n` contributors to one cell cannot
