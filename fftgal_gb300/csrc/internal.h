@@ -105,11 +105,6 @@ int fft2_autotune(FftPlan *p, void *grid, cudaStream_t s, double ms[3]);
 // size, else the in-process cache, else fft2_autotune on `grid`; writes the
 // entry back to `path`.  *source: FFTGAL_PLAN_*; ms: measured times or 0.
 int plan_resolve(FftPlan *p, void *grid, cudaStream_t s, const char *path, bool quiet, int *source, double ms[3]);
-// i-axis pass of two grids fused with the interlacing finish:
-// A <- scale * 0.5 * (A + B * phaseB) * Winv3   (see spectral tables)
-int fft_pass_i_interlace(const FftPlan *p, void *gridA, void *gridB,
-                         const void *phase_tab, const void *winv_tab, double scale,
-                         cudaStream_t s);
 
 // ---- paint -----------------------------------------------------------------
 struct PaintTiling {
