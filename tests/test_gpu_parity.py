@@ -349,6 +349,25 @@ def test_batch_matches_single_calls(fg, graphs):
     _check_batch(fg, g, got, cats, V, los, dK, Nmu)
 
 
+@pytest.mark.parametrize("Ng", [48, 96])
+def test_graph_batch_with_the_general_fft(fg, Ng):
+    """Grid sizes that are not powers of two take the mixed-radix FFT inside
+    the captured graph: each catalog still matches its fftgal_power_f32."""
+    L, Nmu = 400.0, 3
+    los, dK = (0.0, 0.0, 1.0), 2 * np.pi / L
+    cats = [uniform_box(300 + c, n, L) for c, n in enumerate((30_000, 12_000, 45_000))]
+    V = [L ** 3] * len(cats)
+    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
+    got = g.power_batch_f32(cats, V, los, dK, Nmu=Nmu)
+    _check_batch(fg, g, got, cats, V, los, dK, Nmu)
+
+
+def test_batch_needs_fp32_grid(fg):
+    g = fg.Grid(16, 100.0, precision="f64", host_view="lazy")
+    with pytest.raises(RuntimeError):
+        g.power_batch_f32([uniform_box(1, 1000, 100.0)], 100.0 ** 3, (0, 0, 1), 2 * np.pi / 100.0)
+
+
 def test_graph_batches_recapture_and_reuse(fg):
     """Graph batches on one grid across calls: the same captured graphs for
     smaller catalogs, recapture for a larger catalog, other bins or another
