@@ -514,8 +514,11 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, ui
 // cells.  By the bank layout each of the 4 atomic steps is a single
 // shared-memory wavefront (two grids).  The loop is unrolled so that the
 // shared loads of the next particles overlap the atomics of the current one
-// (unrolled by 4: 2 % faster than by 2 at Ng = 1024; one grid with the half
-// warps on alternate particles: 9.5 ms against 11.7 ms with one half idle).
+// (unrolled by 4: 2 % faster than by 2 at Ng = 1024).  One grid: 32
+// particles staged per round by all lanes and the half warps depositing
+// alternate ones took the one-grid tile paint from 11.7 to 6.9 ms at Ng=1024
+// (with the grid count a template parameter of the kernel, which also took
+// the two-grid paint from 12.4 to 11.9 ms).
 // Stencil cells outside the tile (local index kOut) are skipped.
 // slot of particle p of grid g in the stage buffer: the two grids' records
 // interleave so that lanes reading both fall in different banks
@@ -575,9 +578,10 @@ __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, i
 #pragma unroll 4
         for (int p = 0; p < np; ++p) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
     } else {
-        // one grid: the half warps deposit alternate particles
+        // one grid: 32 particles staged in slots 0..31, the half warps
+        // deposit alternate ones
 #pragma unroll 2
-        for (int p = h; p < np; p += 2) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, 0), 0, a, b, lane_off);
+        for (int p = h; p < np; p += 2) deposit_one<FIXED, FAST>(acc, sb, p, 0, a, b, lane_off);
     }
 }
 
@@ -598,6 +602,9 @@ __device__ __forceinline__ int fix_bits_for(uint32_t n) {
 // The next tile's segment offsets are loaded during the write-out, the
 // accumulators are cleared as they are written out, and each warp loads its
 // next batch of records before depositing the current one.
+// NGR = pp.ngrids (1 or 2), a template parameter so that the staging and
+// deposit loops are specialised for one grid or the interlaced pair.
+template <int NGR>
 __global__ void __launch_bounds__(kPaintThreads, 2)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po, unsigned ntiles) {
@@ -618,7 +625,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     __shared__ uint32_t masktab[2][40];
     int tab_te0 = -1, tab_te1 = -1;
 
-    const int Ng = pp.Ng, ngr = pp.ngrids;
+    const int Ng = pp.Ng, ngr = NGR;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
     unsigned tile = blockIdx.x;
     if (tile >= ntiles) return;
@@ -739,25 +746,27 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         const bool fixed = fixbits >= kMinFixBits;
         const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
 
-        // pass B: each warp stages 16 particles (both grids), then deposits
-        // them one by one; the records of the warp's next batch are loaded
-        // before the deposit so their latency hides behind it
+        // pass B: each warp stages 16 particles for both grids (lanes 0..15
+        // grid 0, 16..31 grid 1), or 32 particles for one grid, then deposits
+        // them; the records of the warp's next batch are loaded before the
+        // deposit so their latency hides behind it
         StageBuf &sb = stage[warp];
         const bool fast = !(cyc[0] || cyc[1] || cyc[2]);
-        const int gs = lane / kStageParts;  // lanes 0..15 stage grid 0, 16..31 grid 1
-        const uint32_t bstride = (uint32_t)nwarp * kStageParts;
-        uint32_t base = (uint32_t)warp * kStageParts;
+        const int parts = ngr > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
+        const int gs = ngr > 1 ? lane / kStageParts : 0;
+        const uint32_t bstride = (uint32_t)nwarp * parts;
+        uint32_t base = (uint32_t)warp * parts;
         uint4 rec = make_uint4(0, 0, 0, 0);
         {
-            const uint32_t q = base + (lane & (kStageParts - 1));
-            if (q < total && gs < ngr) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+            const uint32_t q = base + (lane & (parts - 1));
+            if (q < total) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
         }
         for (; base < total; base += bstride) {
-            const uint32_t q = base + (lane & (kStageParts - 1));
-            if (q < total && gs < ngr) {
+            const uint32_t q = base + (lane & (parts - 1));
+            if (q < total) {
                 const uint32_t rw[3] = {rec.x, rec.y, rec.z};
                 const float inv = ldexpf(1.0f, -fb);
-                const int slot = stage_slot(lane & (kStageParts - 1), gs);
+                const int slot = ngr > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
                 int bgv[3], lv[3];
                 uint32_t par = 0;
 #pragma unroll
@@ -807,10 +816,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             }
             __syncwarp();
             {
-                const uint32_t qn = base + bstride + (lane & (kStageParts - 1));
-                if (qn < total && gs < ngr) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
+                const uint32_t qn = base + bstride + (lane & (parts - 1));
+                if (qn < total) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
             }
-            const int np = min((uint32_t)kStageParts, total - base);
+            const int np = min((uint32_t)parts, total - base);
             if (fast) {
                 if (fixed)
                     deposit_all<true, true>(acc, sb, np, ngr, lane);
@@ -1119,10 +1128,14 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
         const size_t smem = kAccBytes + sizeof(StageBuf) * (kPaintThreads / 32) + sizeof(uint32_t) * kBlkN;
-        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         unsigned nb = (unsigned)(2 * num_sms());
         nb = nb < ntiles ? nb : ntiles;
-        paint_coop_kernel<<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+        if (ngrids == 1)
+            paint_coop_kernel<1><<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+        else
+            paint_coop_kernel<2><<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
     } else {
         const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
         FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
