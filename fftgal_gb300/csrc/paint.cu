@@ -626,10 +626,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     int tab_te0 = -1, tab_te1 = -1;
 
     const int Ng = pp.Ng, ngr = NGR;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kPaintThreads / 32;  // launched with kPaintThreads
     unsigned tile = blockIdx.x;
     if (tile >= ntiles) return;
-    for (int e = tid; e < (int)(kAccBytes / 16); e += blockDim.x)
+    for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
         reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
     TileSegs ts;
     {
@@ -672,9 +672,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             int nb[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
-            for (int e = tid; e < kBlkN; e += blockDim.x) blk[e] = 0u;
+            for (int e = tid; e < kBlkN; e += kPaintThreads) blk[e] = 0u;
             __syncthreads();
-            for (uint32_t q = tid; q < total; q += blockDim.x) {
+            for (uint32_t q = tid; q < total; q += kPaintThreads) {
                 const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
                 const uint32_t rw[3] = {r.x, r.y, r.z};
                 int bidx = 0;
@@ -703,7 +703,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             // reuses the stage area.
             uint32_t *tmp = reinterpret_cast<uint32_t *>(stage);
             const int D1 = blk_dim(1), D2 = blk_dim(2);
-            for (int e = tid; e < kBlkN; e += blockDim.x) {
+            for (int e = tid; e < kBlkN; e += kPaintThreads) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 uint32_t v = 0;
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[2] || k + 2 < nb[2]);
@@ -712,7 +712,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 tmp[e] = v;
             }
             __syncthreads();
-            for (int e = tid; e < kBlkN; e += blockDim.x) {
+            for (int e = tid; e < kBlkN; e += kPaintThreads) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 uint32_t v = 0;
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[1] || j + 2 < nb[1]);
@@ -722,7 +722,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             }
             __syncthreads();
             uint32_t mx = 0;
-            for (int e = tid; e < kBlkN; e += blockDim.x) {
+            for (int e = tid; e < kBlkN; e += kPaintThreads) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[0] || i + 2 < nb[0]);
                 if (in) {
