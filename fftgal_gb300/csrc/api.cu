@@ -1058,7 +1058,10 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
     fin.scale = interlace ? 0.5 * H3 : H3;
     if (!interlace) fin.B = nullptr;
     if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
-    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, interlace ? 2 : 3, Vinv, Pshot, tm ? &ev[10] : nullptr,
+    // a single paint with the lazy host view bins the deconvolved field
+    // without storing it (4.3 GB fewer writes at Ng=1024)
+    const int bmode = interlace ? 2 : (g->view == FFTGAL_VIEW_LAZY ? 4 : 3);
+    FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, bmode, Vinv, Pshot, tm ? &ev[10] : nullptr,
                     &fin));
     if (tm) {
         FG_CUDA(cudaEventSynchronize(ev[kStages]));

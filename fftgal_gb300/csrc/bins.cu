@@ -300,6 +300,7 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
 //           (A + B * phase) * W^-1 * scale is written back and binned.
 //   MODE 3: as 2 without an interlacing grid: A <- A * W^-1 * scale (the
 //           deconvolution of a single paint, src/fft.c:236-254).
+//   MODE 4: as 3 with the deconvolved value binned but not written back.
 constexpr int kSlabI = 16, kSlabJ = 16, kSlabK = 32, kSlabRow = 33;
 constexpr int kSlabThreads = 512;  // one warp per slab of a block
 constexpr int kFoldBlocks = 8;
@@ -368,11 +369,11 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
                         const float2 v = make_float2((dv.x + av.x) * wk, (dv.y + av.y) * wk);
                         fin.A[e] = v;
                         pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
-                    } else if (MODE == 3) {
+                    } else if (MODE == 3 || MODE == 4) {
                         const float wk = wfk * fin.w[rr];
                         const float2 av = fin.A[e];
                         const float2 v = make_float2(av.x * wk, av.y * wk);
-                        fin.A[e] = v;
+                        if (MODE == 3) fin.A[e] = v;
                         pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
                     } else if (MODE == 1) {
                         const float2 v = f[e];
@@ -489,8 +490,10 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
             FG_SLAB_LAUNCH(1);
         else if (mode == 2)
             FG_SLAB_LAUNCH(2);
-        else
+        else if (mode == 3)
             FG_SLAB_LAUNCH(3);
+        else
+            FG_SLAB_LAUNCH(4);
 #undef FG_SLAB_LAUNCH
     } else {
         const int Ng_pad = 2 * (s.Ng / 2 + 1);

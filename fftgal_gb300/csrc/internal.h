@@ -229,7 +229,8 @@ struct BinFinish {
 // mode 1: input holds delta (complex), P = |delta|^2 * Vinv - Pshot computed on the fly;
 // mode 2 (FP32): `fin` names both interlacing grids, A <- (A + B phase) W^-1 H^3/2
 // is written back and binned as in mode 1 (`f` unused); mode 3 (FP32): one grid,
-// A <- A W^-1 scale (fin->B, ph32 unused).
+// A <- A W^-1 scale (fin->B, ph32 unused); mode 4 (FP32): as 3 without
+// writing A back (the deconvolved field exists only while it is binned).
 // Results (host): Psum[NK][4] (count-weighted, times Legendre), Pw[NK][Nmu+1].
 // `ev_end` (optional) is recorded right after the binning kernel
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,

@@ -134,7 +134,10 @@ int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const f
  * multipoles and wedges -- the sequence fft_p2g(offset 0) -> fft_x2k(0) ->
  * fft_deconv -> P -> Pl -> Pmu (src/fft.c:57-131,172-181,236-254,
  * src/power.c:12-178).  Half the paint and FFT work of the interlaced call;
- * aliasing is not suppressed. */
+ * aliasing is not suppressed.  With the sync host view the grid then holds
+ * the deconvolved field (grid->f and the device grid); with the lazy view the
+ * device grid keeps the r2c output before deconvolution, which is applied
+ * only while binning. */
 int fftgal_power_single_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
                             double V, int where, const double los[3], double dK, int Nmu,
                             double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
