@@ -116,6 +116,10 @@ SIGNATURES = {
     "fftgal_power_learned_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                            C.c_int, _dp, C.c_double, C.c_int, C.POINTER(C.c_float), _dp, _lp,
                                            _dp, _dp, _lp, _dp]),
+    "fftgal_power_learned_checked_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp,
+                                                   C.c_int, _dp, C.c_double, C.c_int, C.POINTER(C.c_float),
+                                                   C.c_int, C.c_double, _dp, _lp, _dp, _dp, _lp, _dp,
+                                                   C.POINTER(C.c_int), _dp]),
     "fftgal_power_single_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                           C.c_int, _dp, C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_power_rsd_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -437,6 +441,54 @@ class Grid:
                                             K.ctypes.data_as(_dp), N.ctypes.data_as(_lp), P.ctypes.data_as(_dp),
                                             Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))
         return [dict(K=K[c], N=N[c], P=P[c], Kmu=Km[c], Nmu=Nm[c], Pmu=Pm[c]) for c in range(n)]
+
+    def power_learned_f32(self, x, y, z, V: float, los, dK: float, params, Nmu: int = 3,
+                          where: int = MEM_HOST, Np: int | None = None) -> dict:
+        """fftgal_power_learned_f32: one paint, multipoles corrected by the
+        perceptron with parameters ``params`` (fftgal_mlp_nparams() floats)."""
+        if where == MEM_HOST:
+            arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+            ptrs = [a.ctypes.data for a in arrs]
+            Np = len(arrs[0])
+        else:
+            ptrs = [int(x), int(y), int(z)]
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        NK = lib().fftgal_nk(self.Ng, self.L, float(dK))
+        K, N, P = np.zeros(NK), np.zeros(NK, dtype=np.int64), np.zeros((NK, 4))
+        Km, Nm, Pm = np.zeros((NK, Nmu)), np.zeros((NK, Nmu), dtype=np.int64), np.zeros((NK, Nmu))
+        l = _f64(los)
+        _check(lib().fftgal_power_learned_f32(self.p, ptrs[0], ptrs[1], ptrs[2], int(Np), float(V), int(where),
+                                              l.ctypes.data_as(_dp), float(dK), int(Nmu),
+                                              p.ctypes.data_as(C.POINTER(C.c_float)), K.ctypes.data_as(_dp),
+                                              N.ctypes.data_as(_lp), P.ctypes.data_as(_dp), Km.ctypes.data_as(_dp),
+                                              Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp)))
+        return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm)
+
+    def power_learned_checked_f32(self, cats, V, los, dK: float, params, holdout_every: int, tol: float,
+                                  Nmu: int = 3):
+        """fftgal_power_learned_checked_f32 over host catalogs ``cats``:
+        (results, used, disagreement), used[c] 0 learned, 1 judged
+        (interlaced reported), 2 interlaced fallback."""
+        arrs = [[np.ascontiguousarray(a, dtype=np.float32) for a in c] for c in cats]
+        n = len(arrs)
+        ptr = [(C.c_void_p * n)(*[c[a].ctypes.data for c in arrs]) for a in range(3)]
+        Np = np.array([len(c[0]) for c in arrs], dtype=np.int64)
+        Vs = np.ascontiguousarray(np.broadcast_to(np.asarray(V, dtype=np.float64), (n,)))
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        NK = lib().fftgal_nk(self.Ng, self.L, float(dK))
+        K, N, P = np.zeros((n, NK)), np.zeros((n, NK), dtype=np.int64), np.zeros((n, NK, 4))
+        Km, Nm, Pm = np.zeros((n, NK, Nmu)), np.zeros((n, NK, Nmu), dtype=np.int64), np.zeros((n, NK, Nmu))
+        used = np.zeros(n, dtype=np.int32)
+        dis = np.zeros(n)
+        l = _f64(los)
+        _check(lib().fftgal_power_learned_checked_f32(
+            self.p, n, ptr[0], ptr[1], ptr[2], Np.ctypes.data_as(_lp), Vs.ctypes.data_as(_dp), MEM_HOST,
+            l.ctypes.data_as(_dp), float(dK), int(Nmu), p.ctypes.data_as(C.POINTER(C.c_float)), int(holdout_every),
+            float(tol), K.ctypes.data_as(_dp), N.ctypes.data_as(_lp), P.ctypes.data_as(_dp), Km.ctypes.data_as(_dp),
+            Nm.ctypes.data_as(_lp), Pm.ctypes.data_as(_dp), used.ctypes.data_as(C.POINTER(C.c_int)),
+            dis.ctypes.data_as(_dp)))
+        res = [dict(K=K[c], N=N[c], P=P[c], Kmu=Km[c], Nmu=Nm[c], Pmu=Pm[c]) for c in range(n)]
+        return res, used, dis
 
     def power_rsd_f32(self, x, y, z, vx, vy, vz, V: float, los, aH: float, dK: float, Nmu: int = 3,
                       where: int = MEM_HOST, Np: int | None = None) -> dict:

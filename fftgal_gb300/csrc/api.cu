@@ -22,8 +22,10 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <vector>
 
 namespace fg {
@@ -1484,6 +1486,72 @@ extern "C" int fftgal_power_learned_f32(fft_t *grid, const float *x, const float
         const double sc = ok ? den * fftgal_alias_envelope(Kb[b] / kNyq) : 0.0;
         for (int l = 0; l < 4; ++l)
             if (Pl) Pl[4 * b + l] = Pb[4 * b + l] + (l < 3 ? sc * Y[3 * b + l] : 0.0);
+    }
+    return OK;
+}
+
+// Learned mode with the interlaced estimator as judge and fallback: every
+// holdout_every-th catalog (0: none) is measured both ways and reported with
+// its interlaced result; once a judged catalog's learned estimate differs from
+// its interlaced one by more than tol (max over l = 0, 2, 4 and bins with modes
+// below 0.8 k_Nyq of |P_l^learned - P_l^interlaced| / (|P_0^interlaced| +
+// Pshot)), every later catalog runs interlaced.
+extern "C" int fftgal_power_learned_checked_f32(fft_t *grid, int ncat, const float *const *x,
+                                                const float *const *y, const float *const *z, const long *Np,
+                                                const double *V, int where, const double los[3], double dK,
+                                                int Nmu, const float *mlp_params, int holdout_every, double tol,
+                                                double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
+                                                double *Pmu, int *used, double *disagreement) {
+    if (!grid || ncat < 0 || (ncat > 0 && (!x || !y || !z || !Np || !V || !used)) || !mlp_params ||
+        holdout_every < 0 || !(tol >= 0))
+        return set_error(ERR_ARG, "fftgal_power_learned_checked_f32: bad arguments");
+    const int NK = fftgal_nk(grid->Ng, grid->L, dK);
+    if (NK < 1 || Nmu < 1) return set_error(ERR_ARG, "fftgal_power_learned_checked_f32: bad dK or Nmu");
+    const double kNyq = M_PI * grid->Ng / grid->L;
+    const size_t nw = (size_t)NK * Nmu;
+    std::vector<double> Kl(NK), Pll((size_t)NK * 4), Kml(nw), Pml(nw), Ki(NK), Pli((size_t)NK * 4), Kmi(nw), Pmi(nw);
+    std::vector<long> Nl(NK), Nml(nw), Ni(NK), Nmi(nw);
+    bool fallback = false;
+    for (int c = 0; c < ncat; ++c) {
+        if (!x[c] || !y[c] || !z[c] || Np[c] <= 0 || !(V[c] > 0))
+            return set_error(ERR_ARG, "fftgal_power_learned_checked_f32: bad catalog %d", c);
+        if (disagreement) disagreement[c] = NAN;
+        const bool judge = holdout_every > 0 && c % holdout_every == 0;
+        const bool was_fallback = fallback;
+        // the estimate reported for catalog c is in (Ki, Ni, Pli, ...) when
+        // interlaced, in (Kl, Nl, Pll, ...) when learned
+        const bool report_interlaced = was_fallback || judge;
+        if (!was_fallback)
+            FG_TRY(fftgal_power_learned_f32(grid, x[c], y[c], z[c], Np[c], V[c], where, los, dK, Nmu, mlp_params,
+                                            Kl.data(), Nl.data(), Pll.data(), Kml.data(), Nml.data(), Pml.data()));
+        if (report_interlaced)
+            FG_TRY(power_f32_run(grid, x[c], y[c], z[c], nullptr, 0, Np[c], V[c], where, los, dK, Nmu, Ki.data(),
+                                 Ni.data(), Pli.data(), Kmi.data(), Nmi.data(), Pmi.data(), true));
+        if (judge && !was_fallback) {
+            const double Pshot = V[c] / Np[c];
+            double err = 0;
+            for (int b = 0; b < NK; ++b) {
+                if (Ni[b] <= 0 || !(Ki[b] < 0.8 * kNyq) || !std::isfinite(Pli[4 * b])) continue;
+                const double den = fabs(Pli[4 * b]) + Pshot;
+                for (int l = 0; l < 3; ++l) err = std::max(err, fabs(Pll[4 * b + l] - Pli[4 * b + l]) / den);
+            }
+            if (disagreement) disagreement[c] = err;
+            if (err > tol) fallback = true;
+        }
+        used[c] = was_fallback ? 2 : (judge ? 1 : 0);
+        const double *Ks = report_interlaced ? Ki.data() : Kl.data();
+        const long *Ns = report_interlaced ? Ni.data() : Nl.data();
+        const double *Ps = report_interlaced ? Pli.data() : Pll.data();
+        const double *Kms = report_interlaced ? Kmi.data() : Kml.data();
+        const long *Nms = report_interlaced ? Nmi.data() : Nml.data();
+        const double *Pms = report_interlaced ? Pmi.data() : Pml.data();
+        const size_t o1 = (size_t)NK * c, o4 = (size_t)NK * 4 * c, om = nw * c;
+        if (K) std::copy(Ks, Ks + NK, K + o1);
+        if (N) std::copy(Ns, Ns + NK, N + o1);
+        if (Pl) std::copy(Ps, Ps + (size_t)NK * 4, Pl + o4);
+        if (Kmu) std::copy(Kms, Kms + nw, Kmu + om);
+        if (Nmu_count) std::copy(Nms, Nms + nw, Nmu_count + om);
+        if (Pmu) std::copy(Pms, Pms + nw, Pmu + om);
     }
     return OK;
 }

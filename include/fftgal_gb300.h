@@ -201,6 +201,23 @@ int fftgal_power_learned_f32(fft_t *grid, const float *x, const float *y, const 
                              const float *mlp_params, double *K, long *N, double *Pl, double *Kmu,
                              long *Nmu_count, double *Pmu);
 
+/* Learned mode over a list of catalogs (x[c], y[c], z[c], Np[c], V[c]; host or
+ * device memory per `where`) with the interlaced estimator as judge and
+ * fallback: every holdout_every-th catalog (c % holdout_every == 0; 0 = none)
+ * is measured both ways and its interlaced result is reported, with
+ * disagreement[c] = the largest |P_l^learned - P_l^interlaced| /
+ * (|P_0^interlaced| + Pshot) over l = 0, 2, 4 and the bins with modes below
+ * 0.8 k_Nyq; once a disagreement exceeds tol, every later catalog runs
+ * interlaced.  used[c]: 0 learned, 1 interlaced (judged), 2 interlaced
+ * (fallback); disagreement (may be NULL) is NaN where not judged.  Outputs as
+ * fftgal_power_batch_f32, one catalog after another. */
+int fftgal_power_learned_checked_f32(fft_t *grid, int ncat, const float *const *x,
+                                     const float *const *y, const float *const *z, const long *Np,
+                                     const double *V, int where, const double los[3], double dK,
+                                     int Nmu, const float *mlp_params, int holdout_every, double tol,
+                                     double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
+                                     double *Pmu, int *used, double *disagreement);
+
 /* fftgal_power_f32 of the redshift-space catalog: every particle is
  * displaced along the line of sight while it is painted, x + (v . los) / aH
  * los, as gal_rsd forms it (src/gal.c:63-77), so the P.c sequence

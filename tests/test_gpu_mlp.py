@@ -64,3 +64,52 @@ def test_committed_params_correct_single_paint(fg):
         s, l = r["single"], r["learned"]
         assert l["rms_below_0p8"] < 0.5 * s["rms_below_0p8"], r
         assert l["rms_all"] < s["rms_all"], r
+
+
+def _err(a, b, Pshot):
+    den = np.abs(np.nan_to_num(b["P"][:, :1])) + Pshot
+    ok = np.isfinite(b["P"]) & (b["N"][:, None] > 0)
+    return float((np.abs(a["P"] - b["P"]) / den)[ok].max())
+
+
+def test_learned_checked_judge_and_fallback(fg):
+    """fftgal_power_learned_checked_f32: held-out catalogs report the
+    interlaced estimate and their disagreement, the others the learned one;
+    a disagreement above tol switches every later catalog to interlaced.
+    Two runs of one estimator agree to 1e-6 of (|P_0| + Pshot) (the bin sums'
+    atomic order varies); learned ones to 1e-4, as the network's local-slope
+    feature differences neighbouring bins."""
+    import torch
+    from fftgal_gb300 import alias_mlp as a, mocks
+    Ng, L = 128, 1000.0
+    dK, V, los = 2 * np.pi / L, L ** 3, (0.0, 0.0, 1.0)
+    cats = []
+    for seed in range(5):
+        x, y, z, vx, vy, vz = mocks.lognormal_catalog(Ng, L, 3e5, 900 + seed, axes=(2,))
+        cats.append((x.cpu().numpy(), y.cpu().numpy(), (z + vz).cpu().numpy()))
+    torch.cuda.synchronize()
+    params = a.load()
+    g = fg.Grid(Ng, L, precision="f32", host_view="lazy")
+    res, used, dis = g.power_learned_checked_f32(cats, V, los, dK, params, 2, 1e9)
+    assert list(used) == [1, 0, 1, 0, 1]
+    for c, cat in enumerate(cats):
+        Pshot = V / len(cat[0])
+        learned = g.power_learned_f32(*cat, V, los, dK, params)
+        if used[c] == 1:
+            inter = g.power_f32(*cat, V, los, dK)
+            assert _err(res[c], inter, Pshot) <= 1e-6
+            ok = (inter["N"] > 0) & (inter["K"] < 0.8 * np.pi * Ng / L)
+            den = np.abs(inter["P"][:, 0]) + Pshot
+            want = (np.abs(learned["P"][:, :3] - inter["P"][:, :3]) / den[:, None])[ok].max()
+            print("judged", c, dis[c], want)
+            assert abs(dis[c] - want) <= 1e-4
+        else:
+            assert np.isnan(dis[c])
+            e = _err(res[c], learned, Pshot)
+            print("learned", c, e)
+            assert e <= 1e-4
+    res, used, dis = g.power_learned_checked_f32(cats, V, los, dK, params, 2, 0.0)
+    assert list(used) == [1, 2, 2, 2, 2] and dis[0] > 0 and np.all(np.isnan(dis[1:]))
+    assert _err(res[3], g.power_f32(*cats[3], V, los, dK), V / len(cats[3][0])) <= 1e-6
+    res, used, dis = g.power_learned_checked_f32(cats, V, los, dK, params, 0, 0.0)
+    assert list(used) == [0] * 5 and np.all(np.isnan(dis))
