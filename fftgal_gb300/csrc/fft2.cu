@@ -1,4 +1,4 @@
-// Two-level FP32 FFT passes for power-of-two lengths up to 1024 (sm_103a).
+// Two-level FP32 FFT passes for power-of-two lengths up to 2048 (sm_103a).
 //
 // A length N = N1 * N2 transform along a column (or a packed k row) is done
 // as  X[k1 + N1 k2] = sum_n2 W_N2^{n2 k2} W_N^{n2 k1} sum_n1 x[N2 n1 + n2] W_N1^{n1 k1}
@@ -11,9 +11,11 @@
 //           in-register FFT of length N2 and stores X[k1 + N1 k2].
 // One shared-memory round trip per pass (the Stockham kernels of fft.cu take
 // one per radix pass); the row pitches are padded so both shared-memory
-// phases are free of bank conflicts.  Used for the forward r2c k pass and
-// the strided j/i passes of FP32 grids; other lengths and FP64 grids use the
-// general kernels of fft.cu.
+// phases are free of bank conflicts.  Length 2048 on the strided axes is
+// 32 x 64 with the 64-point second step split over lane pairs
+// (fft2_cols2048_kernel).  Used for the forward r2c k pass and the strided
+// j/i passes of FP32 grids; other lengths and FP64 grids use the general
+// kernels of fft.cu.
 #include "internal.h"
 #include "common.cuh"
 
@@ -123,6 +125,65 @@ fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC,
     (void)N;
 }
 
+// ---- strided axis of length 2048 = 32 x 64 ---------------------------------------------
+// Step 1 as fft2_cols_kernel<32, 64> (threads = C * 64).  Step 2's length-64
+// transforms would need 64 complex registers per thread; instead each
+// (column, k1) is taken by a pair of lanes l and l ^ 16, one transforming the
+// even n2 and one the odd n2 with reg_fft<32>, and the final radix-2 step
+//   X[k2] = E[k2] + W_64^k2 O[k2],  X[k2 + 32] = E[k2] - W_64^k2 O[k2]
+// exchanges E and O through shuffles.  Shared pitch P = 32 C + 16 (= 16 mod 32)
+// keeps the step-2 reads of a warp (c, k1 bit, pair half in lane bits 0-4) on
+// 32 distinct banks; the step-1 stores then take two wavefronts.
+__global__ void __launch_bounds__(512)
+fft2_cols2048_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC, const float2 *__restrict__ W,
+                     int sign) {
+    constexpr int N1 = 32, N2 = 64;
+    extern __shared__ __align__(16) float2 S[];
+    const int C = 1 << logC;
+    const int P = N1 * C + 16;
+    const int ncb = (ncols + C - 1) >> logC;
+    const int cb = blockIdx.x % ncb;
+    const long batch = blockIdx.x / ncb;
+    float2 *g = blockIdx.y == 0 ? g0 : g1;
+    const int c0 = cb << logC;
+    float2 *base = g + batch * bs + c0;
+    const int t = threadIdx.x;
+    {
+        const int c = t & (C - 1), n2 = t >> logC;
+        const bool ok = c0 + c < ncols;
+        float2 v[N1];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1)
+            v[n1] = ok ? base[(long)(N2 * n1 + n2) * es + c] : make_float2(0.f, 0.f);
+        reg_fft<N1>(v, sign);
+#pragma unroll
+        for (int k1 = 1; k1 < N1; ++k1)
+            if (n2) v[k1] = cmul(v[k1], twid(W, n2 * k1, sign));
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) S[n2 * P + k1 * C + c] = v[k1];
+    }
+    __syncthreads();
+    // C * N1 tasks for C * N2 / 2 lane pairs: exactly one task per pair
+    const int lane = t & 31, h = lane >> 4;
+    const int task = (t >> 5) * 16 + (lane & 15);
+    const int c = task & (C - 1), k1 = task >> logC;
+    float2 u[32];
+#pragma unroll
+    for (int m = 0; m < 32; ++m) u[m] = S[(2 * m + h) * P + k1 * C + c];
+    reg_fft<32>(u, sign);
+    const bool ok = c0 + c < ncols;
+#pragma unroll
+    for (int k2 = 0; k2 < 32; ++k2) {
+        float2 other;
+        other.x = __shfl_xor_sync(0xffffffffu, u[k2].x, 16);
+        other.y = __shfl_xor_sync(0xffffffffu, u[k2].y, 16);
+        const float2 E = h ? other : u[k2], O = h ? u[k2] : other;
+        const float2 wo = cmul(O, twid(W, 32 * k2, sign));  // W_2048^(32 k2) = W_64^k2
+        const float2 x = h ? csub(E, wo) : cadd(E, wo);
+        if (ok) base[(long)(k1 + N1 * (k2 + 32 * h)) * es + c] = x;
+    }
+}
+
 // ---- k axis, forward r2c: R rows per CTA, threads = R * N2 ---------------------------
 // Each real row of Ng = 2M values is read as M packed complex values
 // z[m] = x[2m] + i x[2m+1]; X[k] = E[k] + W_Ng^k O[k] for k = 0..M.
@@ -218,9 +279,21 @@ static bool split2(int N, int *N1, int *N2) {
     return true;
 }
 
+// strided passes: split2, or 32 x 64 with paired step-2 lanes for N = 2048
+static bool cols_split(int N, int *N1, int *N2, bool *paired) {
+    *paired = N == 2048;
+    if (*paired) {
+        *N1 = 32;
+        *N2 = 64;
+        return true;
+    }
+    return split2(N, N1, N2);
+}
+
 bool fft2_supported(int Ng, int prec) {
     int a, b;
-    return prec == 4 && Ng >= 4 && split2(Ng, &a, &b) && split2(Ng / 2, &a, &b);
+    bool pr;
+    return prec == 4 && Ng >= 4 && cols_split(Ng, &a, &b, &pr) && split2(Ng / 2, &a, &b);
 }
 
 #define FG_COLS_CASE(A, B)                                                                                 \
@@ -244,7 +317,9 @@ static int cols_default_logC(int N2, bool wide) {
     return logC;
 }
 
-static size_t cols_smem(int N1, int N2, int logC) { return (size_t)N2 * (N1 * (1 << logC) + 8) * sizeof(float2); }
+static size_t cols_smem(int N1, int N2, int logC, bool paired = false) {
+    return (size_t)N2 * (N1 * (1 << logC) + (paired ? 16 : 8)) * sizeof(float2);
+}
 
 static int k_default_rows(int N2) {
     int R = 1;  // rows per CTA: threads = R*N2 around 64 (small CTAs, many per SM)
@@ -259,8 +334,10 @@ static size_t k_smem(int N1, int N2, int R) {
 
 bool fft2_valid_shape(int Ng, int which, int v) {
     int N1, N2;
+    bool paired = false;
     const int N = which == 0 ? Ng / 2 : Ng;
-    if (!fft2_supported(Ng, 4) || !split2(N, &N1, &N2)) return false;
+    if (!fft2_supported(Ng, 4) || !(which == 0 ? split2(N, &N1, &N2) : cols_split(N, &N1, &N2, &paired)))
+        return false;
     if (which == 0) {  // k pass: R rows per CTA
         if (v < 1 || v > 64 || (v & (v - 1))) return false;
         const int thr = v * N2;
@@ -268,12 +345,13 @@ bool fft2_valid_shape(int Ng, int which, int v) {
     }
     if (v < 0 || v > 5) return false;  // j or i pass: log2 columns per CTA
     const int thr = (1 << v) * N2;
-    return thr >= 32 && thr <= 512 && cols_smem(N1, N2, v) <= (size_t)device_max_smem();
+    return thr >= 32 && thr <= 512 && cols_smem(N1, N2, v, paired) <= (size_t)device_max_smem();
 }
 
 int fft2_default_shape(int Ng, int which) {
     int N1, N2;
-    if (!split2(which == 0 ? Ng / 2 : Ng, &N1, &N2)) return -1;
+    bool paired = false;
+    if (!(which == 0 ? split2(Ng / 2, &N1, &N2) : cols_split(Ng, &N1, &N2, &paired))) return -1;
     if (which == 0) return k_default_rows(N2);
     const long es = which == 1 ? (long)(Ng / 2 + 1) : (long)Ng * (Ng / 2 + 1);
     return cols_default_logC(N2, es * (long)sizeof(float2) > (1L << 20));
@@ -285,19 +363,28 @@ int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, l
               long nbatch, int sign, cudaStream_t s, int logC_req) {
     FG_TRY(ensure_w32());
     int N1, N2;
-    if (!split2(N, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_cols: N=%d", N);
+    bool paired;
+    if (!cols_split(N, &N1, &N2, &paired)) return set_error(ERR_UNSUPPORTED, "fft2_cols: N=%d", N);
     int logC = cols_default_logC(N2, es * (long)sizeof(float2) > (1L << 20));
     if (logC_req >= 0) {
         const int thr = (1 << logC_req) * N2;
-        if (logC_req > 5 || thr < 32 || thr > 512 || cols_smem(N1, N2, logC_req) > (size_t)device_max_smem())
+        if (logC_req > 5 || thr < 32 || thr > 512 ||
+            cols_smem(N1, N2, logC_req, paired) > (size_t)device_max_smem())
             return set_error(ERR_ARG, "fft2_cols: %d columns per CTA invalid for N=%d", 1 << logC_req, N);
         logC = logC_req;
     }
     const int C = 1 << logC;
     const int threads = C * N2;
-    const size_t smem = cols_smem(N1, N2, logC);
+    const size_t smem = cols_smem(N1, N2, logC, paired);
     const long ncb = ceil_div(ncols, C);
     dim3 grid((unsigned)(ncb * nbatch), ngrids);
+    if (paired) {
+        FG_CUDA(cudaFuncSetAttribute(fft2_cols2048_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fft2_cols2048_kernel<<<grid, threads, smem, s>>>((float2 *)g0, (float2 *)g1, ncols, es, bs, logC,
+                                                         (const float2 *)W, sign);
+        FG_LAUNCHED(1);
+        return OK;
+    }
     FG_COLS_CASE(1, 1)
     FG_COLS_CASE(2, 1)
     FG_COLS_CASE(2, 2)
