@@ -114,7 +114,7 @@ SIGNATURES = {
     "fftgal_plan_valid": (C.c_int, [C.c_int, C.c_int, C.c_int]),
     "fftgal_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "fftgal_fft_columns_f32": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_long, C.c_int,
-                                         C.c_void_p]),
+                                         C.c_int, C.c_void_p]),
     "fftgal_power_learned_f32": (C.c_int, [_P_F, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_double,
                                            C.c_int, _dp, C.c_double, C.c_int, C.POINTER(C.c_float), _dp, _lp,
                                            _dp, _dp, _lp, _dp]),

@@ -893,14 +893,16 @@ extern "C" int fftgal_set_stream(fft_t *grid, void *stream) {
 }
 
 extern "C" int fftgal_fft_columns_f32(int N, void *data, int ncols, long es, long bs, long nbatch, int sign,
-                                      void *stream) {
+                                      int shape, void *stream) {
     if (!data || N < 4 || ncols < 1 || es < 1 || nbatch < 1 || (sign != 1 && sign != -1))
         return set_error(ERR_ARG, "fftgal_fft_columns_f32: bad arguments");
     if (!fft2_supported(N, 4)) return set_error(ERR_UNSUPPORTED, "fftgal_fft_columns_f32: N=%d", N);
+    if (shape != -1 && !fft2_valid_shape(N, 1, shape))
+        return set_error(ERR_ARG, "fftgal_fft_columns_f32: shape %d invalid for N=%d", shape, N);
     FftPlan p;
     FG_TRY(fft_plan_create(&p, N, 4));
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = fft2_cols(N, p.axis.tw, data, data, 1, ncols, es, bs, nbatch, sign, st);
+    int rc = fft2_cols(N, p.axis.tw, data, data, 1, ncols, es, bs, nbatch, sign, st, shape);
     if (rc == OK) rc = cuda_check(cudaStreamSynchronize(st), "fftgal_fft_columns_f32");
     fft_plan_destroy(&p);
     return rc;

@@ -189,10 +189,11 @@ int fftgal_plan_autotune(fft_t *grid, double ms[3]);
  * strided columns of complex FP32 data in GPU memory, with the kernels of the
  * grid's j and i passes: element n of column c (c < ncols) of batch b
  * (b < nbatch) is data[b * bs + n * es + c] (complex units); sign -1
- * forward, +1 backward; stream as cudaStream_t (NULL: legacy default).
- * Returns after the transforms are done. */
+ * forward, +1 backward; shape: -1 for the built-in launch shape, else a
+ * j/i-pass shape of the plan (log2 columns per CTA); stream as cudaStream_t
+ * (NULL: legacy default).  Returns after the transforms are done. */
 int fftgal_fft_columns_f32(int N, void *data, int ncols, long es, long bs, long nbatch, int sign,
-                           void *stream);
+                           int shape, void *stream);
 /* host-only plan file access: 1 and tune[] if `path` holds an entry for the
  * key, 0 if not (or no file); store replaces the key's entry */
 int fftgal_plan_lookup(const char *path, int cc, int sms, int Ng, int prec, int tune[3]);
