@@ -182,8 +182,12 @@ int plan_resolve(FftPlan *p, void *grid, cudaStream_t s, const char *path, bool 
         std::lock_guard<std::mutex> lk(g_cache_mu);
         g_cache[{k.cc, k.sms, p->Ng, p->prec}] = {tun[0], tun[1], tun[2]};
     }
-    FG_TRY(plan_store(path, k.cc, k.sms, p->Ng, p->prec, tun, ms, k.name));
-    if (!quiet) fprintf(stderr, "fft_init() exported plan to %s\n", path);
+    // a plan file that cannot be written costs the next run a measurement,
+    // not this run its grid: warn and go on with the shapes just found
+    if (plan_store(path, k.cc, k.sms, p->Ng, p->prec, tun, ms, k.name) != OK)
+        fprintf(stderr, "fft_init() could not export the plan to %s: %s\n", path, fftgal_last_error());
+    else if (!quiet)
+        fprintf(stderr, "fft_init() exported plan to %s\n", path);
     return OK;
 }
 

@@ -101,3 +101,13 @@ def test_fp64_and_untunable_sizes_use_builtin_plans(fg, tmp_path):
     g = fg.Grid(64, L_BOX, wisdom=str(path), precision="f64")
     assert g.plan_info()["source"] == fg.PLAN_BUILTIN
     assert not path.exists()
+
+
+def test_unwritable_plan_file_is_not_fatal(fg, tmp_path):
+    """A plan file in a directory that does not exist cannot be written: the
+    grid is still made, with the measured shapes, and nothing is created."""
+    path = tmp_path / "no_such_dir" / "plan"
+    _, f = _kgrid(fg, 32, path)
+    _, f_est = _kgrid(fg, 32, "FFTW_ESTIMATE")
+    np.testing.assert_array_equal(f, f_est)
+    assert not path.exists()
