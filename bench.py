@@ -361,6 +361,8 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}",
                        "fft_plan": {"source": ["built-in", "measured", "plan file", "process cache"][
                            grid.plan_info()["source"]], "tune": grid.plan_info()["tune"]},
+                       "particles_per_s": round(value * Np, 1),
+                       "particles_per_s_e2e": round(e2e * Np, 1),
                        "stages_ms": stage_table,
                        "step_roofline": {"algorithmic_bytes": step_algo,
                                          "achieved_GBs": round(step_algo / (ms / args.steps / 1000) / 1e9, 1),
