@@ -1284,8 +1284,11 @@ static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const
             g->d_batch[b] = nullptr;
         }
         g->batch_cap = 0;
-        for (int b = 0; b < 2; ++b) FG_CUDA(cudaMalloc(&g->d_batch[b], sizeof(float) * 3 * maxNp));
-        g->batch_cap = (size_t)3 * maxNp;
+        // 1/8 headroom: a later batch with slightly larger catalogs reuses
+        // the buffers (and, with graphs, the captured graphs)
+        const size_t room = (size_t)maxNp + (size_t)maxNp / 8 + 1024;
+        for (int b = 0; b < 2; ++b) FG_CUDA(cudaMalloc(&g->d_batch[b], sizeof(float) * 3 * room));
+        g->batch_cap = 3 * room;
     }
     const long capNp = (long)(g->batch_cap / 3);
     FG_TRY(ensure_aux(g));
@@ -1305,15 +1308,17 @@ static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const
         if (g->h_scal) cudaFreeHost(g->h_scal);
         g->h_scal = nullptr;
         g->h_scal_cap = 0;
-        FG_CUDA(cudaMallocHost(&g->h_scal, sizeof(DevScalars) * ncat));
-        g->h_scal_cap = ncat;
+        const size_t cap = (size_t)ncat + (size_t)ncat / 2 + 16;  // headroom for growing batches
+        FG_CUDA(cudaMallocHost(&g->h_scal, sizeof(DevScalars) * cap));
+        g->h_scal_cap = cap;
     }
     if ((size_t)ncat * geo->acc_len > g->h_acc_cap) {
         if (g->h_acc) cudaFreeHost(g->h_acc);
         g->h_acc = nullptr;
         g->h_acc_cap = 0;
-        FG_CUDA(cudaMallocHost(&g->h_acc, sizeof(double) * ncat * geo->acc_len));
-        g->h_acc_cap = (size_t)ncat * geo->acc_len;
+        const size_t cap = ((size_t)ncat + (size_t)ncat / 2 + 16) * geo->acc_len;
+        FG_CUDA(cudaMallocHost(&g->h_acc, sizeof(double) * cap));
+        g->h_acc_cap = cap;
     }
     // recapture whenever a buffer, table, plan or bin layout the graphs name changed
     std::vector<uint64_t> key;
@@ -1420,8 +1425,11 @@ extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const 
             g->d_batch[b] = nullptr;
         }
         g->batch_cap = 0;
-        for (int b = 0; b < 2; ++b) FG_CUDA(cudaMalloc(&g->d_batch[b], sizeof(float) * 3 * maxNp));
-        g->batch_cap = (size_t)3 * maxNp;
+        // 1/8 headroom: a later batch with slightly larger catalogs reuses
+        // the buffers (and, with graphs, the captured graphs)
+        const size_t room = (size_t)maxNp + (size_t)maxNp / 8 + 1024;
+        for (int b = 0; b < 2; ++b) FG_CUDA(cudaMalloc(&g->d_batch[b], sizeof(float) * 3 * room));
+        g->batch_cap = 3 * room;
     }
     const int NK = fftgal_nk(grid->Ng, grid->L, dK);
     if (NK < 1) return set_error(ERR_ARG, "fftgal_power_batch_f32: bad dK");
