@@ -11,8 +11,7 @@ the network learns them divided by the envelope e(k / k_Nyq) = u^6 / (1 + u^6)
 and clipped to +-5 (``scaled_targets``): the raw targets span seven decades
 from k << k_Nyq to the corners of the cube, and the bins past about 1.5 k_Nyq
 hold few modes whose differences are noise.  The gradient and Adam kernels run
-on the GPU; ``forward_np`` / ``grad_np`` restate them in FP64 for the gradient
-check.
+on the GPU (their FP64 restatement for the parity tests is oracle/mlp.py).
 
     python -m fftgal_gb300.alias_mlp train --pairs 2000 --out params.npy
     python -m fftgal_gb300.alias_mlp eval --params params.npy --ng 1024 --np 1e8
@@ -61,37 +60,6 @@ def init_params(seed: int = 0) -> np.ndarray:
             fan_in, fan_out = SHAPES[k]
             p[o:o + n] = rng.normal(0.0, math.sqrt(1.0 / fan_in), n) * (0.1 if k == "W4" else 1.0)
     return p
-
-
-def forward_np(p, X):
-    """FP64 restatement of mlp_forward_kernel."""
-    w = {k: v.astype(np.float64) for k, v in unpack(p).items()}
-    a1 = np.tanh(X @ w["W1"] + w["b1"])
-    a2 = np.tanh(a1 @ w["W2"] + w["b2"])
-    a3 = np.tanh(a2 @ w["W3"] + w["b3"])
-    return a3 @ w["W4"] + w["b4"], (a1, a2, a3)
-
-
-def grad_np(p, X, T):
-    """FP64 restatement of mlp_grad_kernel: gradient and value of the mean
-    over samples of |y - t|^2."""
-    X = np.asarray(X, dtype=np.float64)
-    T = np.asarray(T, dtype=np.float64)
-    n = len(X)
-    w = {k: v.astype(np.float64) for k, v in unpack(p).items()}
-    y, (a1, a2, a3) = forward_np(p, X)
-    r = y - T
-    loss = float((r * r).sum() / n)
-    d4 = 2.0 * r / n
-    d3 = (d4 @ w["W4"].T) * (1 - a3 * a3)
-    d2 = (d3 @ w["W3"].T) * (1 - a2 * a2)
-    d1 = (d2 @ w["W2"].T) * (1 - a1 * a1)
-    g = {"W4": a3.T @ d4, "b4": d4.sum(0), "W3": a2.T @ d3, "b3": d3.sum(0), "W2": a1.T @ d2, "b2": d2.sum(0),
-         "W1": X.T @ d1, "b1": d1.sum(0)}
-    out = np.zeros(NPARAMS)
-    for k, (o, n_) in LAYOUT.items():
-        out[o:o + n_] = g[k].ravel()
-    return out, loss
 
 
 class Trainer:

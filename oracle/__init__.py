@@ -14,6 +14,9 @@ Two oracles live here:
   FFTW/GSL headers (oracle/Makefile target ``ref``).  It exists only where the
   reference sources are present; it is used to pin ``Oracle`` and to write the
   golden fixtures under tests/golden/.
+
+``oracle.mlp`` restates the learned-correction perceptron's forward pass and
+gradient in FP64 (numpy) for the parity tests of the GPU kernels.
 """
 from __future__ import annotations
 

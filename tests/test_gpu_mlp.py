@@ -1,9 +1,12 @@
 """Learned aliasing correction kernels (csrc/mlp.cu): the GPU gradient of the
-mean squared error against an FP64 restatement (fftgal_gb300.alias_mlp.grad_np,
-itself checked against finite differences), the forward kernel, and a short
-Adam run that fits a smooth target."""
+mean squared error against the FP64 restatement oracle/mlp.py (itself checked
+against finite differences in tests/test_mlp_oracle.py), the forward kernel,
+a short Adam run that fits a smooth target, the committed parameters, and
+the learned mode with the interlaced estimator as judge."""
 import numpy as np
 import pytest
+
+from oracle import mlp as mlp_ref
 
 pytestmark = pytest.mark.gpu
 
@@ -27,7 +30,7 @@ def test_gradient_against_fp64(fg):
     tr = a.Trainer(p)
     g, loss = tr.grad(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"))
     g = g.cpu().numpy().astype(np.float64)
-    g64, loss64 = a.grad_np(p, X, T)
+    g64, loss64 = mlp_ref.grad(p, X, T)
     assert abs(loss - loss64) <= 1e-5 * loss64
     assert np.linalg.norm(g - g64) <= 1e-4 * np.linalg.norm(g64)
     for k, (o, n) in a.LAYOUT.items():  # every layer, not just the norm
@@ -40,7 +43,7 @@ def test_forward_against_fp64(fg):
     p = a.init_params(6)
     X = rng.standard_normal((500, a.IN)).astype(np.float32)
     y = a.forward_gpu(p, X)
-    y64, _ = a.forward_np(p, X.astype(np.float64))
+    y64, _ = mlp_ref.forward(p, X.astype(np.float64))
     assert np.abs(y - y64).max() <= 1e-5 * max(1.0, np.abs(y64).max())
 
 
