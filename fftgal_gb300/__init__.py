@@ -469,7 +469,7 @@ class Grid:
     def power_learned_checked_f32(self, cats, V, los, dK: float, params, holdout_every: int, tol: float,
                                   Nmu: int = 3):
         """fftgal_power_learned_checked_f32 over host catalogs ``cats``:
-        (results, used, disagreement), used[c] 0 learned, 1 judged
+        (results, used, disagreement), used[c] 0 learned, 1 checked
         (interlaced reported), 2 interlaced fallback."""
         arrs = [[np.ascontiguousarray(a, dtype=np.float32) for a in c] for c in cats]
         n = len(arrs)

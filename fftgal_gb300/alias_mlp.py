@@ -220,7 +220,7 @@ def load(path: str = DEFAULT_PARAMS) -> np.ndarray:
 
 def evaluate(params, Ng: int, Np: float, n_mocks: int = 2, seed: int = 12345, mock_n: int | None = None):
     """Fresh-seed mocks: errors of single-paint and single-paint + MLP against
-    the interlaced estimate (the judge), in units of den, for k < 0.8 k_Nyq
+    the interlaced estimate (the reference measurement), in units of den, for k < 0.8 k_Nyq
     and over all bins; and the two pipelines' device times."""
     import torch
     from . import Grid, MEM_DEVICE, lib, _check, _dp, _lp

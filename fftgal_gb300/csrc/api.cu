@@ -1514,9 +1514,9 @@ extern "C" int fftgal_power_learned_f32(fft_t *grid, const float *x, const float
     return OK;
 }
 
-// Learned mode with the interlaced estimator as judge and fallback: every
+// Learned mode checked against the interlaced estimator, with fallback: every
 // holdout_every-th catalog (0: none) is measured both ways and reported with
-// its interlaced result; once a judged catalog's learned estimate differs from
+// its interlaced result; once a checked catalog's learned estimate differs from
 // its interlaced one by more than tol (max over l = 0, 2, 4 and bins with modes
 // below 0.8 k_Nyq of |P_l^learned - P_l^interlaced| / (|P_0^interlaced| +
 // Pshot)), every later catalog runs interlaced.
@@ -1540,18 +1540,18 @@ extern "C" int fftgal_power_learned_checked_f32(fft_t *grid, int ncat, const flo
         if (!x[c] || !y[c] || !z[c] || Np[c] <= 0 || !(V[c] > 0))
             return set_error(ERR_ARG, "fftgal_power_learned_checked_f32: bad catalog %d", c);
         if (disagreement) disagreement[c] = NAN;
-        const bool judge = holdout_every > 0 && c % holdout_every == 0;
+        const bool check = holdout_every > 0 && c % holdout_every == 0;
         const bool was_fallback = fallback;
         // the estimate reported for catalog c is in (Ki, Ni, Pli, ...) when
         // interlaced, in (Kl, Nl, Pll, ...) when learned
-        const bool report_interlaced = was_fallback || judge;
+        const bool report_interlaced = was_fallback || check;
         if (!was_fallback)
             FG_TRY(fftgal_power_learned_f32(grid, x[c], y[c], z[c], Np[c], V[c], where, los, dK, Nmu, mlp_params,
                                             Kl.data(), Nl.data(), Pll.data(), Kml.data(), Nml.data(), Pml.data()));
         if (report_interlaced)
             FG_TRY(power_f32_run(grid, x[c], y[c], z[c], nullptr, 0, Np[c], V[c], where, los, dK, Nmu, Ki.data(),
                                  Ni.data(), Pli.data(), Kmi.data(), Nmi.data(), Pmi.data(), true));
-        if (judge && !was_fallback) {
+        if (check && !was_fallback) {
             const double Pshot = V[c] / Np[c];
             double err = 0;
             for (int b = 0; b < NK; ++b) {
@@ -1562,7 +1562,7 @@ extern "C" int fftgal_power_learned_checked_f32(fft_t *grid, int ncat, const flo
             if (disagreement) disagreement[c] = err;
             if (err > tol) fallback = true;
         }
-        used[c] = was_fallback ? 2 : (judge ? 1 : 0);
+        used[c] = was_fallback ? 2 : (check ? 1 : 0);
         const double *Ks = report_interlaced ? Ki.data() : Kl.data();
         const long *Ns = report_interlaced ? Ni.data() : Nl.data();
         const double *Ps = report_interlaced ? Pli.data() : Pll.data();

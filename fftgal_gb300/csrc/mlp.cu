@@ -2,7 +2,7 @@
 // hidden units, linear output, FP32) that maps the single-paint multipoles of
 // a k bin to the interlaced ones, and its training kernels (mean squared
 // error, batch gradients, Adam).  No counterpart in the reference: the
-// interlaced estimator (fft_p2k, src/fft.c:257-276) is the target and judge.
+// interlaced estimator (fft_p2k, src/fft.c:257-276) is the training target and the measure of its error.
 //
 // Features of bin b (fftgal_alias_features), den = |P0| + Pshot:
 //   k / k_Nyq, Pshot / den, P2 / den, P4 / den, d ln den / d ln k (neighbours);

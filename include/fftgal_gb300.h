@@ -211,14 +211,14 @@ int fftgal_power_learned_f32(fft_t *grid, const float *x, const float *y, const 
                              long *Nmu_count, double *Pmu);
 
 /* Learned mode over a list of catalogs (x[c], y[c], z[c], Np[c], V[c]; host or
- * device memory per `where`) with the interlaced estimator as judge and
+ * device memory per `where`) checked against the interlaced estimator, with
  * fallback: every holdout_every-th catalog (c % holdout_every == 0; 0 = none)
  * is measured both ways and its interlaced result is reported, with
  * disagreement[c] = the largest |P_l^learned - P_l^interlaced| /
  * (|P_0^interlaced| + Pshot) over l = 0, 2, 4 and the bins with modes below
  * 0.8 k_Nyq; once a disagreement exceeds tol, every later catalog runs
- * interlaced.  used[c]: 0 learned, 1 interlaced (judged), 2 interlaced
- * (fallback); disagreement (may be NULL) is NaN where not judged.  Outputs as
+ * interlaced.  used[c]: 0 learned, 1 interlaced (checked), 2 interlaced
+ * (fallback); disagreement (may be NULL) is NaN where not checked.  Outputs as
  * fftgal_power_batch_f32, one catalog after another. */
 int fftgal_power_learned_checked_f32(fft_t *grid, int ncat, const float *const *x,
                                      const float *const *y, const float *const *z, const long *Np,

@@ -2,7 +2,7 @@
 mean squared error against the FP64 restatement oracle/mlp.py (itself checked
 against finite differences in tests/test_mlp_oracle.py), the forward kernel,
 a short Adam run that fits a smooth target, the committed parameters, and
-the learned mode with the interlaced estimator as judge."""
+the learned mode checked against the interlaced estimator."""
 import numpy as np
 import pytest
 
@@ -58,7 +58,7 @@ def test_adam_fits_a_smooth_target(fg):
 
 def test_committed_params_correct_single_paint(fg):
     """The committed parameters, on fresh mocks outside the training seeds:
-    single paint + perceptron is closer to the interlaced estimate (the judge)
+    single paint + perceptron is closer to the interlaced estimate
     than the single paint alone: by more than 2x in rms below 0.8 k_Nyq, and
     over all bins (whose rms the noise of the few-mode corner bins dominates)."""
     from fftgal_gb300 import alias_mlp as a
@@ -75,7 +75,7 @@ def _err(a, b, Pshot):
     return float((np.abs(a["P"] - b["P"]) / den)[ok].max())
 
 
-def test_learned_checked_judge_and_fallback(fg):
+def test_learned_checked_and_fallback(fg):
     """fftgal_power_learned_checked_f32: held-out catalogs report the
     interlaced estimate and their disagreement, the others the learned one;
     a disagreement above tol switches every later catalog to interlaced.
@@ -104,7 +104,7 @@ def test_learned_checked_judge_and_fallback(fg):
             ok = (inter["N"] > 0) & (inter["K"] < 0.8 * np.pi * Ng / L)
             den = np.abs(inter["P"][:, 0]) + Pshot
             want = (np.abs(learned["P"][:, :3] - inter["P"][:, :3]) / den[:, None])[ok].max()
-            print("judged", c, dis[c], want)
+            print("checked", c, dis[c], want)
             assert abs(dis[c] - want) <= 1e-4
         else:
             assert np.isnan(dis[c])
