@@ -860,7 +860,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 uint32_t *a0 = acc + kPadK + li * kSI;
                 uint32_t *a1 = a0 + kGS;
                 for (int lj = 0; lj < te1; ++lj, o0 += rstride, o1 += rstride, a0 += kSJ, a1 += kSJ) {
-                    float v0 = 0.f, v1 = 0.f;
+                    // padding cells take 0 x scale, as the reference scales the
+                    // whole padded grid (src/fft.c:127-129): NaN for an empty catalog
+                    float v0 = 0.f * sc0, v1 = 0.f * sc1;
                     if (lane < te2) {
                         const uint32_t c0 = a0[lane];
                         a0[lane] = 0u;
@@ -880,8 +882,8 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                         }
                     }
                     if (lane + 32 < rowlen) {  // row padding beyond a full 32-cell tile
-                        if (!po.accumulate[0]) o0[lane + 32] = 0.f;
-                        if (ngr > 1 && !po.accumulate[1]) o1[lane + 32] = 0.f;
+                        if (!po.accumulate[0]) o0[lane + 32] = 0.f * sc0;
+                        if (ngr > 1 && !po.accumulate[1]) o1[lane + 32] = 0.f * sc1;
                     }
                 }
             }
@@ -949,8 +951,8 @@ paint_tile_f64_kernel(PaintParams pp, const uint32_t *__restrict__ off,
         for (int e = threadIdx.x; e < ncell; e += blockDim.x) {
             const int lk = e % rowlen, lj = (e / rowlen) % ts.te[1], li = e / (rowlen * ts.te[1]);
             const long gi = ((long)(ts.t0[0] + li) * Ng + (ts.t0[1] + lj)) * pp.Ng_pad + ts.t0[2] + lk;
-            double v = 0;
-            if (lk < ts.te[2]) v = __dmul_rn(acc[g * kT3 + (li * 16 + lj) * 32 + lk], sc);
+            // padding cells: 0 x scale, like the reference's scaling of the whole grid
+            const double v = __dmul_rn(lk < ts.te[2] ? acc[g * kT3 + (li * 16 + lj) * 32 + lk] : 0.0, sc);
             if (accu) {
                 if (lk < ts.te[2]) out[gi] = __dadd_rn(out[gi], v);
             } else {

@@ -443,3 +443,32 @@ def test_super_sample_modes(fg, oracle_lib, prec, Ng, Nsub, sphere):
     assert scale > 0
     err = np.abs(got - want).max() / scale
     assert err <= tol, f"max error {err:.2e} of {scale:.3e}"
+
+
+@pytest.mark.parametrize("prec,rel", [("f64", 1e-12), ("f32", 2e-5)])
+def test_empty_and_wrapped_catalogs(fg, oracle_lib, prec, rel):
+    """Edge catalogs through fft_p2g (src/fft.c:57-131) against the oracle:
+    no particles (NaN everywhere, as the reference's final scaling by
+    1/nbar = inf gives), one particle at the origin, one on the upper
+    box edge, and particles several boxes away on either side (the cell index
+    wraps mod Ng), with and without a grid offset."""
+    Ng, L = 16, 100.0
+    V = L ** 3
+    cases = [
+        (np.zeros(0), np.zeros(0), np.zeros(0)),
+        (np.array([0.0]), np.array([0.0]), np.array([0.0])),
+        (np.array([L - 1e-9]), np.array([L * 0.5]), np.array([L - 1e-9])),
+        (np.array([-0.3 * L, 2.7 * L, 0.01]), np.array([1.7 * L, -1.2 * L, 99.99]), np.array([2.5 * L, 0.5, -3.1 * L])),
+    ]
+    for x, y, z in cases:
+        for offset in ([0.0, 0.0, 0.0], [0.5, 0.5, 0.5]):
+            g = fg.Grid(Ng, L, precision=prec)
+            off = g.p2g(fg.Catalog(x, y, z, V), offset)
+            o = oracle_lib.Oracle(Ng, L)
+            want_off = o.p2g(x, y, z, V, offset)
+            np.testing.assert_array_equal(off, want_off)
+            if len(x) == 0:  # the reference scales by 1/nbar = inf: NaN everywhere
+                assert np.isnan(np.array(o.f)).all()
+                assert np.isnan(np.array(g.f)).all()
+            else:
+                grid_close(np.array(g.f), np.array(o.f), rel)
