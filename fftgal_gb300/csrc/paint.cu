@@ -25,8 +25,8 @@
 // every such step touch 32 distinct banks.  Sums are 32-bit fixed point with a
 // per-tile scale 2^-s, s the largest value for which no cell can exceed 2^32 (a
 // particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
-// total bounds every cell, and only where that bound costs precision does a
-// first pass count particles per 4^3-cell block.  Integer sums are order
+// total bounds every cell, and only where that bound leaves fewer than 20
+// fraction bits does a first pass count particles per 4^3-cell block.  Integer sums are order
 // independent, so the painted grid is bit-reproducible run to run.
 // FP64 grids (paint_tile_f64_kernel) reproduce the reference's FP64 weight
 // arithmetic op for op and accumulate in FP64, one thread per particle.
@@ -62,6 +62,12 @@ constexpr size_t kAccBytes = (sizeof(uint32_t) * 2 * kGS + 15) / 16 * 16;
 // largest fixed-point scale: products stay below 2^22 so the FMA trick of
 // deposit4 converts them to integers exactly
 constexpr int kMaxFixBits = 23;
+// the per-block count that can raise a dense tile's scale runs only when its
+// particle total leaves fewer bits than this: at >= 20 fraction bits a
+// deposit rounds by at most 2^-21 of a unit weight, far inside FP32 grid
+// accuracy, so the extra pass over the tile's records (about 1 ms of the
+// tile paint for a 1e8-galaxy lognormal mock at Ng=1024) buys nothing there
+constexpr int kBlockCountBelow = 20;
 // FP64 shared layout: dense [16][16][32]
 constexpr int kT3 = 16 * 16 * 32;
 // per-tile block counts: 4^3-cell blocks over the tile plus a 4-cell margin
@@ -664,11 +670,11 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         }
 
         // fixed-point scale: the tile's particle total bounds every cell's
-        // contributor count; only when that bound costs precision are the
-        // particles counted per 4^3 block of grid-0 base cells (over the tile
+        // contributor count; only when that bound leaves fewer than
+        // kBlockCountBelow bits are the particles counted per 4^3 block of grid-0 base cells (over the tile
         // plus a 4-cell margin, or the whole periodic axis when one tile spans it)
         int fixbits = fix_bits_for(total);
-        if (fixbits < kMaxFixBits) {
+        if (fixbits < kBlockCountBelow) {
             int nb[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
