@@ -60,4 +60,7 @@ def test_device_catalog_ordered_after_torch_stream(fg):
                          where=fg.MEM_DEVICE, Np=int(x.numel()))
         rh = g.power_f32(x.cpu().numpy(), y.cpu().numpy(), zr.cpu().numpy(), L ** 3, (0, 0, 1), dK, Nmu=3)
         ok = rh["N"] > 0
-        np.testing.assert_allclose(rd["P"][ok], rh["P"][ok], rtol=1e-5, atol=1e-3)
+        # errors in units of |P_0| + Pshot: the bin sums' atomic order varies
+        # between runs, and P_6 near a zero crossing cancels terms ~1e4 larger
+        den = np.abs(rh["P"][ok][:, :1]) + L ** 3 / x.numel()
+        assert (np.abs(rd["P"][ok] - rh["P"][ok]) / den).max() <= 1e-6
