@@ -25,7 +25,7 @@
 // every such step touch 32 distinct banks.  Sums are 32-bit fixed point with a
 // per-tile scale 2^-s, s the largest value for which no cell can exceed 2^32 (a
 // particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
-// total bounds every cell, and only where that bound leaves fewer than 20
+// total bounds every cell, and only where that bound leaves fewer than 21
 // fraction bits does a first pass count particles per 4^3-cell block.  Integer sums are order
 // independent, so the painted grid is bit-reproducible run to run.
 // FP64 grids (paint_tile_f64_kernel) reproduce the reference's FP64 weight
@@ -63,11 +63,13 @@ constexpr size_t kAccBytes = (sizeof(uint32_t) * 2 * kGS + 15) / 16 * 16;
 // deposit4 converts them to integers exactly
 constexpr int kMaxFixBits = 23;
 // the per-block count that can raise a dense tile's scale runs only when its
-// particle total leaves fewer bits than this: at >= 20 fraction bits a
-// deposit rounds by at most 2^-21 of a unit weight, far inside FP32 grid
-// accuracy, so the extra pass over the tile's records (about 1 ms of the
-// tile paint for a 1e8-galaxy lognormal mock at Ng=1024) buys nothing there
-constexpr int kBlockCountBelow = 20;
+// particle total leaves fewer bits than this (tiles of more than about 6900
+// particles): at >= 21 fraction bits a deposit rounds by at most 2^-22 of a
+// unit weight, inside FP32 grid accuracy even where the deconvolution
+// amplifies the noise of the corner bins, so the extra pass over the tile's
+// records (most of 1 ms of the tile paint for a 1e8-galaxy lognormal mock at
+// Ng=1024) is skipped for moderately dense tiles
+constexpr int kBlockCountBelow = 21;
 // FP64 shared layout: dense [16][16][32]
 constexpr int kT3 = 16 * 16 * 32;
 // per-tile block counts: 4^3-cell blocks over the tile plus a 4-cell margin
