@@ -16,6 +16,9 @@ stores its outputs:
   uniform_ng128.npz  the uniform-box configuration: 1e6 particles uniform in
                      [0,1000)^3 (splitmix64 seed 1, FP64), Ng=128, interlaced,
                      dK=2pi/L: the Pl and Pmu tables for 4 lines of sight.
+  gal_rsd_wrap.npz   gal_rsd for 4 lines of sight (one not normalised) x 2
+                     values of aH, and gal_wrap, on 400 particles spread over
+                     three box lengths with Gaussian velocities.
 """
 from __future__ import annotations
 
@@ -100,9 +103,38 @@ def uniform_ng128():
     np.savez_compressed(os.path.join(HERE, "uniform_ng128.npz"), **out)
 
 
+def gal_rsd_wrap():
+    import ctypes as C
+    lib = RefLib.lib()
+    L, n = 100.0, 400
+    x, y, z = uniform_box(7, n, 3 * L, lo=-L)
+    rng = np.random.default_rng(7)  # velocities: any reproducible values do
+    vx, vy, vz = (rng.standard_normal(n) * 40.0 for _ in range(3))
+    out = {"L": L, "pos": np.stack([x, y, z]), "vel": np.stack([vx, vy, vz])}
+    dp = C.POINTER(C.c_double)
+    los_set = [(0.0, 0.0, 1.0), (1.0, 1.0, 0.0), (0.3, -0.2, 0.9), (2.0, 0.0, 0.0)]
+    out["los_set"] = np.array(los_set)
+    out["aH_set"] = np.array([1.0, 0.7])
+    for il, los in enumerate(los_set):
+        for ia, aH in enumerate((1.0, 0.7)):
+            gal = RefGal(x, y, z, L ** 3, vel=(vx, vy, vz))
+            l = np.array(los, dtype=np.float64)  # gal_rsd normalises it in place
+            d = lib.gal_rsd(gal.p, l.ctypes.data_as(dp), aH)
+            g = d.contents
+            out[f"rsd_los{il}_ah{ia}"] = np.stack([np.ctypeslib.as_array(getattr(g, a), shape=(n,)).copy()
+                                                   for a in ("x", "y", "z")])
+            lib.gal_free(d)
+    gal = RefGal(x, y, z, L ** 3)
+    lib.gal_wrap(gal.p, L)
+    g = gal.p.contents
+    out["wrap"] = np.stack([np.ctypeslib.as_array(getattr(g, a), shape=(n,)).copy() for a in ("x", "y", "z")])
+    np.savez_compressed(os.path.join(HERE, "gal_rsd_wrap.npz"), **out)
+
+
 if __name__ == "__main__":
     if not available():
         sys.exit("reference build missing: run `make -C oracle ref` first")
     small_cases()
     uniform_ng128()
+    gal_rsd_wrap()
     print("golden fixtures written to", HERE)
