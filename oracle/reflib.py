@@ -67,6 +67,12 @@ class RefLib:
             lib.gal_rsd.restype = P_G
             lib.gal_rsd.argtypes = [P_G, _dp, C.c_double]
             lib.gal_wrap.argtypes = [P_G, C.c_double]
+            lib.gal_subbox.restype = P_G
+            lib.gal_subbox.argtypes = [P_G, _dp, C.c_double]
+            lib.gal_subsphere.restype = P_G
+            lib.gal_subsphere.argtypes = [P_G, _dp, C.c_double]
+            lib.gal_loadqpm_cubic.restype = P_G
+            lib.gal_loadqpm_cubic.argtypes = [C.c_char_p, C.c_double]
             lib.free.argtypes = [C.c_void_p]
             cls._lib = lib
         return cls._lib
