@@ -135,3 +135,28 @@ def test_alias_envelope_and_scaled_targets():
     e = a.envelope(X[:, 0].astype(np.float64))
     np.testing.assert_allclose(S, np.clip(T / e[:, None], -5, 5), rtol=1e-6)
     assert S[1, 2] == -5 and S[2, 0] == 5
+
+
+def declared_arities():
+    out = {}
+    for dirpath, _, files in os.walk(INCLUDE):
+        for f in files:
+            if not f.endswith(".h"):
+                continue
+            text = open(os.path.join(dirpath, f)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            text = re.sub(r"#define[^\n]*", "", text)
+            for m in re.finditer(r"^[A-Za-z_][\w \t\*]*?\b([A-Za-z_]\w*)\s*\(([^;{}]*)\)\s*;", text, re.M):
+                if m.group(0).lstrip().startswith("static"):
+                    continue
+                params = " ".join(m.group(2).split())
+                out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header_arities(built):
+    """Every function the headers declare has as many arguments in the ctypes
+    table (fftgal_gb300.SIGNATURES) as in its C prototype."""
+    wrong = {n: (k, len(built.SIGNATURES[n][1])) for n, k in declared_arities().items()
+             if n in built.SIGNATURES and len(built.SIGNATURES[n][1]) != k}
+    assert not wrong, wrong
