@@ -45,7 +45,8 @@ int fftgal_set_host_view(fft_t *grid, int mode);
 int fftgal_sync_host(fft_t *grid);
 int fftgal_sync_device(fft_t *grid);
 /* run the grid's work on an existing CUDA stream (cudaStream_t), or NULL to
- * return to the library's own stream */
+ * return to the library's own non-blocking stream (for the legacy default
+ * stream pass cudaStreamLegacy, not 0) */
 int fftgal_set_stream(fft_t *grid, void *cuda_stream);
 void *fftgal_get_stream(fft_t *grid);
 /* suppress (1) or restore (0) the per-call timing lines on stderr; the
@@ -117,11 +118,12 @@ int fftgal_dl_sub(fft_t *grid, int sphere, int Nsub, int nlos, const double *los
  * behind the computation.  Outputs are the fftgal_power_f32 outputs of each
  * catalog one after another: K[ncat*NK], N[ncat*NK], Pl[ncat*NK*4],
  * Kmu/Nmu_count/Pmu[ncat*NK*Nmu] (any may be NULL).  Holds two device buffers
- * of 3 * max(Np) floats until fft_free.
+ * of 3 * (max(Np) + max(Np)/8) floats until fft_free (later batches of up to
+ * that many particles per catalog reuse them).
  * By default (FFTGAL_GRAPHS unset or not "0", or fftgal_set_graphs(grid, 1))
  * each catalog's device work runs as one CUDA graph launch: the sequence is
- * captured once per upload buffer (again when the largest Np, the bins or a
- * buffer change) with the kernels reading each catalog's count and scales
+ * captured once per upload buffer (again when a catalog outgrows the buffers,
+ * or the bins or a buffer change) with the kernels reading each catalog's count and scales
  * from device memory; the host waits once per batch, not once per catalog.
  * Per-stage timers (fftgal_stage_times) are not recorded in that mode. */
 int fftgal_set_graphs(fft_t *grid, int on);
