@@ -3,16 +3,24 @@
 Workload (one step = one catalog): Np = 1e8 FP32 particles in a 1000 Mpc/h
 periodic box, Ng = 1024 grid, PCS paint of both interlacing grids, r2c FFT of
 both, offset phase + average + PCS deconvolution, multipoles l = 0,2,4(,6)
-and 3 mu wedges with dK = 2 pi / L.  Positions are seeded synthetic catalogs
-generated on the GPU (uniform, or the lognormal RSD mock with --mock lognormal).
+and 3 mu wedges with dK = 2 pi / L.  The catalog is the seeded uniform box of
+tests/golden/catalogs.py (splitmix64, seed 20240: the same FP32 positions on
+every machine), whose FP64 reference answer is tests/golden/headline_ng1024.npz;
+``--mock lognormal`` times a clustered redshift-space mock instead.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints ONE JSON line (rank 0).  `value` = catalogs/s with positions already in
 HBM (CUDA events on the launching stream, max over ranks); `e2e` = the same
 call with positions in pinned host memory (host->device copy inside the timed
-region, bins read back every step).  `--impl reference` times the FP64 CPU
-oracle (the reference algorithm restated in C, oracle/) on the host cores.
+region, bins read back every step); `parity` = the timed call's P_l and wedges
+against the FP64 answer (the committed reference tables, and the FP64 oracle
+run live on this host's CPU on the same catalog); `cpu_baseline` = that live
+FP64 run, one full catalog on one core.  ``--impl reference`` times the FP64
+CPU path (the reference algorithm restated in C, oracle/) on full catalogs,
+one single-threaded process per host core that memory allows.
+With ``--gpus N`` (N > 1) and no WORLD_SIZE in the environment the script
+starts itself under torch.distributed.run with N ranks, one GPU each.
 """
 from __future__ import annotations
 
@@ -20,6 +28,7 @@ import argparse
 import json
 import math
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -28,14 +37,17 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
 NG, L_BOX, NP = 1024, 1000.0, 100_000_000
+SEED = 20240  # the uniform catalog of tests/golden/headline_ng1024.npz
 LOS = (0.0, 0.0, 1.0)
 NMU = 3
 METRIC = "catalogs/s at Ng=1024,1e8 gal (P0/2/4 err<=1e-4 vs FP64); % HBM roofline"
+GOLDEN = os.path.join(ROOT, "tests", "golden", "headline_ng1024.npz")
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -49,7 +61,10 @@ def parse():
                     help="plan file of the FFT autotuner (default: one in the temporary directory)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only warmup+this many steps, no e2e/cpu legs (for ncu)")
-    return ap.parse_args()
+    ap.add_argument("--launch-check", action="store_true",
+                    help="exercise the N-rank launch and the max-over-ranks reduction without a GPU "
+                         "(gloo) and print the JSON line")
+    return ap.parse_args(argv)
 
 
 def peaks():
@@ -59,6 +74,42 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# N ranks from one command line
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def relaunch_command(args, argv) -> list | None:
+    """The torch.distributed.run command that runs this script on args.gpus
+    ranks, or None when this process is already a rank (WORLD_SIZE set), runs
+    one GPU, or runs the CPU reference arm (rank 0 only, no relaunch)."""
+    if "WORLD_SIZE" in os.environ or args.gpus <= 1 or args.impl == "reference":
+        return None
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+            "--master-addr", "127.0.0.1", f"--master-port={_free_port()}", os.path.abspath(__file__)] + list(argv)
+
+
+def launch_check(args):
+    """One line from N gloo ranks: the launch path and max_over_ranks without a GPU."""
+    import torch.distributed as dist
+    from fftgal_gb300 import worklist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        dist.init_process_group("gloo")
+    t = worklist.max_over_ranks(1.0 + rank)
+    ranks = worklist.gather_tables({rank: {"rank": rank, "local_rank": int(os.environ.get("LOCAL_RANK", "0"))}},
+                                   world)
+    if rank == 0:
+        print(json.dumps({"launch_check": True, "n_gpus": world, "max_over_ranks": t, "ranks": ranks}), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 # ---------------------------------------------------------------------------
@@ -118,100 +169,130 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU oracle baseline (bounded sample, extrapolated to the full workload)
-def cpu_sample(seed: int = 1, Ng: int = 256, scale: int = 64):
-    """Time the FP64 oracle (p2k + P + Pl + Pmu, src/fft.c:257-276,
-    src/power.c:12-178 restated in C) on an Ng grid with Np/scale particles
-    (scale = (1024/Ng)^3 keeps the full workload's particle density) and
-    extrapolate to Ng=1024, 1e8: particle, grid and binning work x scale, FFT
-    work x scale x log(1024^3)/log(Ng^3) (N log N).
-    Returns (seconds per full catalog, sample seconds)."""
+# catalogs
+def host_catalog(Ng: int, Np: int, seed: int, mock: str):
+    """FP32 x, y, z (numpy) of the benchmark catalog: the seeded uniform box,
+    or a lognormal redshift-space mock (256^3 field, z-RSD with aH = 1)."""
     import numpy as np
+    if mock == "uniform":
+        from catalogs import uniform_box_f32
+        return uniform_box_f32(seed, Np, L_BOX)
+    from lognormal import lognormal_catalog
+    x, y, z, vx, vy, vz = lognormal_catalog(seed, 256, L_BOX, Np)
+    return tuple(np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z + vz))
+
+
+# ---------------------------------------------------------------------------
+# FP64 CPU path (test infrastructure: the oracle restates src/fft.c and
+# src/power.c; it is the checker and the CPU baseline, never the product)
+def oracle_catalog_run(Ng: int, Np: int, seed: int, mock: str, los, dK: float, nmu: int, warm: bool = True):
+    """The P.c sequence fft_p2k -> P -> Pl -> Pmu (src/app/P.c:55-66) of the
+    FP64 oracle on the benchmark catalog (FP32 positions widened to FP64),
+    single-threaded.  Returns (result dict, seconds of the path, timestamps)."""
     import oracle
-    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
-    from catalogs import uniform_box
-    n = int(NP) // scale
-    x, y, z = uniform_box(seed, n, L_BOX)
+    x, y, z = host_catalog(Ng, Np, seed, mock)
     V = L_BOX ** 3
-    t0 = time.perf_counter()
+    if warm:  # page in the library and its code paths on a tiny grid
+        oracle.power_spectrum(16, L_BOX, x[:1000], y[:1000], z[:1000], los, dK, Nmu=nmu, V=V)
+    x, y, z = (a.astype("float64") for a in (x, y, z))
+    t0 = time.monotonic()
     g = oracle.Oracle(Ng, L_BOX)
     g.p2k(x, y, z, V)
-    g.power(n, V)
-    g.pl(LOS, 2 * math.pi / L_BOX)
-    g.pmu(LOS, 2 * math.pi / L_BOX, NMU)
-    t_all = time.perf_counter() - t0
-    # one FFT alone, to split the N log N part from the linear part
-    rnd = np.random.default_rng(seed).standard_normal(g.f.shape)
-    g.f[:] = rnd
-    t1 = time.perf_counter()
-    g.x2k(0)
-    t_fft = time.perf_counter() - t1
-    lin = max(t_all - 2 * t_fft, 0.0)
-    full = lin * scale + 2 * t_fft * scale * (math.log2(NG ** 3) / math.log2(Ng ** 3))
-    return full, t_all + t_fft
+    g.power(len(x), V)
+    K, N, P, _, _ = g.pl(los, dK)
+    Km, Nm, Pm, _, _ = g.pmu(los, dK, nmu)
+    t1 = time.monotonic()
+    return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm), t1 - t0, (t0, t1)
 
 
-def _cpu_worker(args):
-    seed, Ng = args
-    return cpu_sample(seed, Ng, (NG // Ng) ** 3)
+def _oracle_proc(args_tuple, barrier, queue):
+    """--impl reference worker: build the catalog, wait for the others, time one catalog."""
+    Ng, Np, seed, mock, los, dK, nmu = args_tuple
+    import oracle
+    from catalogs import uniform_box_f32  # noqa: F401  (imported before the barrier)
+    x, y, z = host_catalog(Ng, Np, seed, mock)
+    V = L_BOX ** 3
+    oracle.power_spectrum(16, L_BOX, x[:1000], y[:1000], z[:1000], los, dK, Nmu=nmu, V=V)
+    x, y, z = (a.astype("float64") for a in (x, y, z))
+    barrier.wait()
+    t0 = time.monotonic()
+    g = oracle.Oracle(Ng, L_BOX)
+    g.p2k(x, y, z, V)
+    g.power(len(x), V)
+    g.pl(los, dK)
+    g.pmu(los, dK, nmu)
+    queue.put((t0, time.monotonic()))
+
+
+def _host_memory_gb() -> float:
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable:"):
+                return int(ln.split()[1]) / 2 ** 20
+    except Exception:
+        pass
+    return 16.0
+
+
+def oracle_bytes(Ng: int, Np: int) -> float:
+    """Host memory of one FP64 oracle catalog run: the grid and its
+    interlacing copy, FP64 and FP32 positions, and numpy temporaries."""
+    G8 = Ng * Ng * 2 * (Ng // 2 + 1) * 8
+    return 2 * G8 + Np * (24 + 12) + 2 * 2 ** 30
 
 
 def run_reference(args):
-    """--impl reference: the CPU path on all host cores (one single-threaded
-    oracle process per core, the reference's one-process-per-mock model)."""
+    """--impl reference: the FP64 CPU path on full catalogs of the workload,
+    one single-threaded oracle process per host core that memory allows (the
+    reference's one-process-per-mock model, src/app/job_P.sh:22-26), started
+    together after each has built its catalog.  value = catalogs finished / wall."""
     import multiprocessing as mp
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    Ng, Np = args.ng, int(args.np)
+    dK = 2 * math.pi / L_BOX
     cores = os.cpu_count() or 1
-    # keep every process's memory (~0.35 GB at Ng=256) well inside the host
-    try:
-        import psutil
-        mem_gb = psutil.virtual_memory().available / 2 ** 30
-        cores = max(1, min(cores, int(mem_gb // 1.0)))
-    except Exception:
-        pass
+    mem = _host_memory_gb()
+    nproc = max(1, min(cores, int(0.8 * mem * 2 ** 30 // oracle_bytes(Ng, Np))))
     ctx = mp.get_context("spawn")
-    times = []
-    with ctx.Pool(cores) as pool:
-        for w in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            res = pool.map(_cpu_worker, [(100 + w * cores + c, 256) for c in range(cores)])
-            wall = time.perf_counter() - t0
-            if w >= args.warmup:
-                # catalogs per second across the concurrent processes
-                times.append(sum(1.0 / r[0] for r in res))
-    value = statistics.median(times)
+    barrier = ctx.Barrier(nproc + 1)
+    queue = ctx.Queue()
+    procs = [ctx.Process(target=_oracle_proc, args=((Ng, Np, SEED, args.mock, LOS, dK, NMU), barrier, queue))
+             for _ in range(nproc)]
+    for p in procs:
+        p.start()
+    barrier.wait()
+    t0 = time.monotonic()
+    spans = [queue.get() for _ in range(nproc)]
+    wall = max(s[1] for s in spans) - t0
+    for p in procs:
+        p.join()
+    per = [s[1] - s[0] for s in spans]
+    value = nproc / wall
+    sample = (f"{nproc} full catalogs run concurrently (Ng={Ng}, Np={Np:.0e} {args.mock}, seed {SEED}), "
+              f"FP64 oracle fft_p2k+P+Pl+Pmu, one process per core, {wall:.1f} s wall; "
+              f"per catalog {min(per):.1f}-{max(per):.1f} s")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "catalogs/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (uniform, seeded)",
-        "config": {"workload": f"interlaced P_l + 3 wedges, Ng={NG}, Np=1e8, L={L_BOX:g}",
-                   "sample": "Ng=256, Np=1.5625e6 per process, extrapolated x64 (FFT x64x30/24)"},
-        "cpu_baseline": {"value": value, "unit": "catalogs/s", "cores": cores, "kind": "port",
-                         "sample": "FP64 oracle restating src/fft.c + src/power.c, Ng=256 with Np/64 per "
-                                   "process, one process per core, extrapolated to Ng=1024/1e8"},
+        "n_gpus": 0, "n_gpus_requested": args.gpus, "cores": nproc,
+        "steps": nproc, "steps_requested": args.steps, "warmup": 1,
+        "warmup_note": "one Ng=16 pass per process before the timed catalog",
+        "ms_per_step": 1000.0 * wall / nproc, "timed_region_s": wall,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (uniform, seeded splitmix64: the catalog of the GPU arm)",
+        "config": {"workload": workload_name(Ng, Np), "Ng": Ng, "Np": Np, "mock": args.mock,
+                   "host_memory_gb": round(mem, 1), "host_cores": cores},
+        "cpu_baseline": {"value": value, "unit": "catalogs/s", "cores": nproc, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "catalogs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
 
 
 # ---------------------------------------------------------------------------
-def make_catalog(torch, Np: int, seed: int, mock: str, dev):
-    """(3, N) FP32 positions on the device: a uniform box, or a lognormal
-    mock (256^3 field, Zel'dovich velocities, redshift space along z) with
-    about Np particles."""
-    if mock == "uniform":
-        g = torch.Generator(device=dev)
-        g.manual_seed(seed)
-        return torch.rand((3, Np), generator=g, device=dev, dtype=torch.float32) * L_BOX
-    import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
-    from lognormal import lognormal_catalog
-    x, y, z, vx, vy, vz = lognormal_catalog(seed, 256, L_BOX, Np)
-    pos = np.stack([x, y, z + vz]).astype(np.float32)  # gal_rsd along z with aH = 1
-    return torch.from_numpy(pos).to(dev)
+def workload_name(Ng: int, Np: int) -> str:
+    return (f"interlaced PCS P_l (l=0,2,4,6) + {NMU} mu-wedges, Ng={Ng}, Np={Np:.0e}, L={L_BOX:g}, dK=2pi/L, "
+            f"FP32 positions+grids, FP64 bin sums")
 
 
 def algorithmic_bytes(Ng: int, Np: int):
@@ -232,27 +313,67 @@ def algorithmic_bytes(Ng: int, Np: int):
     }
 
 
+def parity_block(res, Ng: int, Np: int, mock: str, live):
+    """The timed call's result against the FP64 answers: the committed
+    reference tables (uniform catalog at the headline size) and the live
+    oracle run on this host."""
+    import numpy as np
+    import parity
+    Pshot = L_BOX ** 3 / Np
+    out = {"criterion": "mode counts exact; P0/2/4 and wedges within 1e-4 of |P0|+Pshot for k<0.8 kNyq; "
+                        "every bin within 1e-3"}
+    if mock == "uniform" and Ng == NG and Np == NP and os.path.exists(GOLDEN):
+        z = np.load(GOLDEN)
+        e = parity.errors(res, parity.golden_result(z, "uniform", 0, NMU), Pshot, Ng, L_BOX)
+        e["pass"] = parity.passes(e)
+        e["source"] = "tests/golden/headline_ng1024.npz (reference fft_p2k/P/Pl/Pmu, FP64)"
+        out["vs_reference_tables"] = e
+    if live is not None:
+        e = parity.errors(res, live, Pshot, Ng, L_BOX)
+        e["pass"] = parity.passes(e)
+        e["source"] = "FP64 oracle on this host, same catalog"
+        out["vs_live_oracle"] = e
+    return out
+
+
 def run_ours(args):
     import numpy as np
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    Ng, Np = args.ng, int(args.np)
+    dK = 2 * math.pi / L_BOX
+    V = L_BOX ** 3
+
+    # the FP64 CPU run (cpu_baseline and live parity) starts before any CUDA
+    # call, in a spawned process, and runs while the GPU legs are timed
+    pool = live_job = None
+    if rank == 0 and not args.no_cpu_baseline and not args.profile_steps:
+        if oracle_bytes(Ng, Np) < 0.8 * _host_memory_gb() * 2 ** 30:
+            import multiprocessing as mp
+            pool = mp.get_context("spawn").Pool(1)
+            live_job = pool.apply_async(oracle_catalog_run, (Ng, Np, SEED, args.mock, LOS, dK, NMU))
+
     import torch
     import torch.distributed as dist
     import fftgal_gb300 as fg
     from fftgal_gb300 import worklist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         dist.init_process_group("nccl")
+    if torch.cuda.device_count() <= local:
+        raise SystemExit(f"bench: rank {rank} needs GPU {local}, {torch.cuda.device_count()} visible")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
-    Ng, Np = args.ng, int(args.np)
-    dK = 2 * math.pi / L_BOX
-    V = L_BOX ** 3
 
-    pos = make_catalog(torch, Np, 1234 + rank, args.mock, dev)
-    Np = int(pos.shape[1])
+    hx = host_catalog(Ng, Np, SEED, args.mock)
+    Np = len(hx[0])
+    host = torch.empty((3, Np), dtype=torch.float32, pin_memory=True)
+    for a in range(3):
+        host[a].numpy()[:] = hx[a]
+    del hx
+    pos = host.to(dev)
     # the FFT launch shapes come from the autotuner's plan file (measured on
     # the first run on a device, like FFTW_MEASURE wisdom)
     plan = args.plan or os.path.join(tempfile.gettempdir(), f"fftgal_gb300_plan_rank{local}.txt")
@@ -299,8 +420,6 @@ def run_ours(args):
     grid.set_timing(False)
 
     # e2e: positions in pinned host memory, copied every step
-    host = torch.empty((3, Np), dtype=torch.float32, pin_memory=True)
-    host.copy_(pos)
     hp = [host[a].numpy() for a in range(3)]
     # fftgal_power_batch_f32: one catalog per step, each copied host -> device
     # inside the timed region (overlapping the previous catalog's computation)
@@ -308,7 +427,7 @@ def run_ours(args):
     barrier()
     k2 = max(3, args.steps)  # one catalog per timed step, as the device-resident leg
     e0.record(stream)
-    grid.power_batch_f32([hp] * k2, V, LOS, dK, Nmu=NMU)
+    res_e2e = grid.power_batch_f32([hp] * k2, V, LOS, dK, Nmu=NMU)
     e1.record(stream)
     barrier()
     ms2 = worklist.max_over_ranks(e0.elapsed_time(e1))
@@ -340,23 +459,27 @@ def run_ours(args):
                        "GBs": (round(algo[k] / (avg[k] / 1000.0) / 1e9, 1) if algo.get(k) and avg[k] > 0 else None)}
                    for k in algo}
 
-    out = None
     if rank == 0:
-        cpu = None
-        if not args.no_cpu_baseline:
-            full, wall = cpu_sample(1, 512, 8)
-            cpu = {"value": 1.0 / full, "unit": "catalogs/s", "cores": 1, "kind": "port",
-                   "sample": f"FP64 oracle (src/fft.c + src/power.c restated), Ng=512, Np=1.25e7 uniform, "
-                             f"{wall:.1f}s, extrapolated to Ng=1024/1e8 (x8, FFT x8x30/27)"}
+        cpu = live = None
+        if live_job is not None:
+            live, secs, _ = live_job.get()
+            pool.close()
+            pool.join()
+            cpu = {"value": 1.0 / secs, "unit": "catalogs/s", "cores": 1, "kind": "port",
+                   "sample": f"one full catalog of this workload (Ng={Ng}, Np={Np:.0e} {args.mock}, seed {SEED}, "
+                             f"positions widened to FP64): FP64 oracle restating src/fft.c + src/power.c, "
+                             f"fft_p2k+P+Pl+Pmu, {secs:.1f} s on 1 core"}
+        par = parity_block(res, Ng, Np, args.mock, live)
+        par["e2e_matches_device_resident"] = bool(
+            np.array_equal(res_e2e[-1]["P"], res["P"]) and np.array_equal(res_e2e[-1]["Pmu"], res["Pmu"]))
         out = {
             "metric": METRIC, "value": value, "unit": "catalogs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": ("synthetic (uniform, seeded, generated on the GPU)" if args.mock == "uniform" else
-                     "synthetic (lognormal mock with z-RSD, seeded, numpy)"),
-            "config": {"workload": f"interlaced PCS P_l (l=0,2,4,6) + {NMU} mu-wedges, Ng={Ng}, Np={Np:.0e}, "
-                                   f"L={L_BOX:g}, dK=2pi/L, FP32 positions+grids, FP64 bin sums",
-                       "Ng": Ng, "Np": Np, "los": LOS, "mock": args.mock,
+            "data": (f"synthetic (uniform box, splitmix64 seed {SEED}, FP32, generated on the host)"
+                     if args.mock == "uniform" else "synthetic (lognormal mock with z-RSD, seeded, numpy)"),
+            "config": {"workload": workload_name(Ng, Np),
+                       "Ng": Ng, "Np": Np, "los": LOS, "mock": args.mock, "seed": SEED,
                        "l2": "inputs larger than L2 (two 4.3 GB grids per step)",
                        "parallelism": f"replicas x{world}",
                        "fft_plan": {"source": ["built-in", "measured", "plan file", "process cache"][
@@ -376,7 +499,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "clocks": clocks,
-            "check": {"P0_k5": float(res["P"][5, 0]), "Pshot": V / Np, "N_k5": int(res["N"][5])},
+            "parity": par,
         }
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -384,9 +507,19 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def main():
-    args = parse()
-    if args.impl == "reference":
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    args = parse(argv)
+    cmd = relaunch_command(args, argv)
+    if cmd is not None:
+        if not args.launch_check:
+            import torch
+            if torch.cuda.device_count() < args.gpus:
+                raise SystemExit(f"bench: --gpus {args.gpus} but {torch.cuda.device_count()} GPUs visible")
+        sys.exit(subprocess.call(cmd))
+    if args.launch_check:
+        launch_check(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -919,6 +919,18 @@ extern "C" int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms
     return OK;
 }
 
+extern "C" int fftgal_fft_slab_planes(fft_t *grid, int planes) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    if (planes >= 0) {
+        if (planes > 0 && !fft2_supported(grid->Ng, g->prec))
+            return set_error(ERR_UNSUPPORTED, "slabs need the two-level FP32 kernels (power-of-two Ng, FP32 grid)");
+        g->fft.kj_planes = planes;
+        ++g->version;
+    }
+    return g->fft.kj_planes;
+}
+
 extern "C" int fftgal_plan_autotune(fft_t *grid, double ms[3]) {
     if (!grid) return set_error(ERR_ARG, "null grid");
     Grid *g = G(grid);
@@ -1054,9 +1066,15 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
     FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, ngr, st, tm ? ev + 2 : nullptr,
                  vel ? &rsd : nullptr));
     void *grids[2] = {g->d_f, g->d_aux};
-    FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
-    if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
-    FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
+    // k and j passes slab by slab (the fft_k stage then times both, fft_j is empty)
+    if (g->fft.kj_planes > 0) {
+        FG_TRY(fft_pass_kj(&g->fft, grids, ngr, st));
+        if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
+    } else {
+        FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
+        if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
+        FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
+    }
     if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
     FG_TRY(fft_pass_i(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
@@ -1076,9 +1094,11 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
     fin.scale = interlace ? 0.5 * H3 : H3;
     if (!interlace) fin.B = nullptr;
     if (tm) FG_CUDA(cudaEventRecord(ev[9], st));
-    // a single paint with the lazy host view bins the deconvolved field
-    // without storing it (4.3 GB fewer writes at Ng=1024)
-    const int bmode = interlace ? 2 : (g->view == FFTGAL_VIEW_LAZY ? 4 : 3);
+    // with the lazy host view the finished (or deconvolved) field is binned
+    // without being stored (4.3 GB fewer writes at Ng=1024); the grid's
+    // contents are then unspecified until the next paint or import
+    const bool keep = g->view != FFTGAL_VIEW_LAZY;
+    const int bmode = interlace ? (keep ? 2 : 5) : (keep ? 3 : 4);
     FG_TRY(bin_pass(grid, los, dK, Nmu, &geo, Psum, Pw, bmode, Vinv, Pshot, tm ? &ev[10] : nullptr,
                     &fin));
     if (tm) {
@@ -1211,8 +1231,7 @@ static int enqueue_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cud
     FG_TRY(paint(&g->tiling, &g->scratch, 4, d, d + capNp, d + 2 * capNp, 4, capNp, Ng / grid->L, spec, 2, st,
                  nullptr, nullptr, g->d_scal + b));
     void *grids[2] = {g->d_f, g->d_aux};
-    FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
-    FG_TRY(fft_pass_j(&g->fft, grids, 2, -1, st));
+    FG_TRY(fft_pass_kj(&g->fft, grids, 2, st));
     FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
     BinFinish fin;
     fin.A = g->d_f;
@@ -1220,7 +1239,8 @@ static int enqueue_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cud
     fin.ph32 = dual_tab32(g);
     fin.w32 = winv_tab32(g);
     fin.scale = 0.5 * H3_of(g);
-    return bin_power_launch(geo, 2, 0, 0, st, &fin, g->d_scal + b);
+    // the lazy host view bins the finished field without storing it
+    return bin_power_launch(geo, g->view == FFTGAL_VIEW_LAZY ? 5 : 2, 0, 0, st, &fin, g->d_scal + b);
 }
 
 static int capture_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cudaGraphExec_t *exec, int *nkern) {
@@ -1327,6 +1347,7 @@ static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const
                           geo->d_acc,      geo->d_thr,        g->d_tab,       g->d_scal};
     for (const void *q : ptrs) key_push(key, (uintptr_t)q);
     key_push(key, capNp);
+    key_push(key, g->view);
     for (int w = 0; w < 3; ++w) key_push(key, g->fft.tune[w]);
     key_push(key, spec.NK);
     key_push(key, Nmu);

@@ -410,13 +410,18 @@ int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, l
         return OK;                                                                                         \
     }
 
-int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s, int R_req) {
+int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s, int R_req,
+               long row0, long nrows_req) {
     FG_TRY(ensure_w32());
     const int M = Ng / 2;
     int N1, N2;
     if (!split2(M, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_k_r2c: Ng=%d", Ng);
     const int Ng_pad = 2 * (M + 1);
-    const long nrows = (long)Ng * Ng;
+    const long nrows = nrows_req >= 0 ? nrows_req : (long)Ng * Ng - row0;
+    if (row0 < 0 || nrows < 1 || row0 + nrows > (long)Ng * Ng)
+        return set_error(ERR_ARG, "fft2_k_r2c: rows [%ld, %ld) outside the grid", row0, row0 + nrows);
+    g0 = static_cast<float *>(g0) + row0 * Ng_pad;
+    g1 = static_cast<float *>(g1) + row0 * Ng_pad;
     int R = k_default_rows(N2);
     if (R_req > 0) {
         if (!fft2_valid_shape(Ng, 0, R_req))

@@ -73,6 +73,11 @@ struct FftPlan {
     // autotuner or a plan file: [0] k-pass rows per CTA (0 = built-in),
     // [1] j-pass and [2] i-pass log2 columns per CTA (-1 = built-in)
     int tune[3] = {0, -1, -1};
+    // forward r2c of FP32 grids: the k and j passes run on slabs of this many
+    // i planes (of two grids; a single grid takes twice as many), k pass then
+    // j pass per slab, so that the j pass finds the k pass's output in L2
+    // (0: one slab, the whole grid)
+    int kj_planes = 0;
 };
 
 int fft_plan_create(FftPlan *p, int Ng, int prec);
@@ -85,12 +90,17 @@ int fft_c2r(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_k_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
 int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
+// the forward k and j passes, slab by slab of p->kj_planes i planes
+int fft_pass_kj(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
+// i planes per slab of fft_pass_kj whose k-pass output of `ngrids` FP32
+// grids fits about half of the L2 cache (0: the whole grid fits)
+int fft_kj_default_planes(int Ng, int ngrids);
 // two-level FP32 kernels (fft2.cu) for power-of-two Ng in [4, 1024]
 bool fft2_supported(int Ng, int prec);
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
               long nbatch, int sign, cudaStream_t s, int logC_req = -1);
 int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s,
-               int R_req = 0);
+               int R_req = 0, long row0 = 0, long nrows = -1);
 // launch shape `v` of pass `which` (0 = k rows per CTA, 1 = j / 2 = i log2
 // columns per CTA) is launchable for Ng; the built-in choice of each pass
 bool fft2_valid_shape(int Ng, int which, int v);
@@ -230,13 +240,14 @@ struct BinFinish {
 // mode 2 (FP32): `fin` names both interlacing grids, A <- (A + B phase) W^-1 H^3/2
 // is written back and binned as in mode 1 (`f` unused); mode 3 (FP32): one grid,
 // A <- A W^-1 scale (fin->B, ph32 unused); mode 4 (FP32): as 3 without
-// writing A back (the deconvolved field exists only while it is binned).
+// writing A back (the deconvolved field exists only while it is binned);
+// mode 5 (FP32): as 2 without writing A back.
 // Results (host): Psum[NK][4] (count-weighted, times Legendre), Pw[NK][Nmu+1].
 // `ev_end` (optional) is recorded right after the binning kernel
 int bin_power(BinGeometry *g, const void *f, int prec, int mode, double Vinv, double Pshot,
               double *Psum, double *Pw, cudaStream_t st, cudaEvent_t *ev_end = nullptr,
               const BinFinish *fin = nullptr);
-// the launches of bin_power (FP32, modes 2 and 3) without the read-back: the
+// the launches of bin_power (FP32, modes 2 to 5) without the read-back: the
 // sums stay in g->d_acc ([NK][4 + Nmu + 1] doubles); with `ds` the kernel
 // takes Vinv and Pshot from device memory
 int bin_power_launch(BinGeometry *g, int mode, double Vinv, double Pshot, cudaStream_t st, const BinFinish *fin,

@@ -1,9 +1,9 @@
 // fftgal_power_bins_noalloc: multipoles and wedges of a k-space grid that is
 // already in GPU memory, for callers that cannot allocate GPU memory -- code
 // running inside a host framework that owns every device allocation (a
-// caching allocator, a memory pool shared with other work), a stream-capture
-// or real-time context where cudaMalloc would serialise or fail, or an
-// embedding that has handed out all device memory in advance.
+// caching allocator, a memory pool shared with other work), or an embedding
+// that has handed out all device memory in advance, where a cudaMalloc would
+// fail or take memory the framework counts on.
 //
 // It is a variant of the binning kernels of bins.cu whose scratch (the
 // per-bin sums, mode counts, k-bin thresholds and the normalised outputs) is
@@ -12,7 +12,14 @@
 // counts and mean |k| that bins.cu caches per geometry are accumulated here in
 // the same pass instead.  Every call shares the array: the accumulators are
 // cleared at the start of each call, and calls whose work overlaps on the GPU
-// (other host threads, other streams) race on it.
+// (other host threads, other streams) race on it.  The call waits for its
+// stream (cudaStreamSynchronize) before it returns the tables.
+//
+// Limits: NK <= 2048 k bins (the fixed scratch), Nmu <= 16 wedges, and the
+// per-CTA shared accumulators -- FP32 power sums [4 + Nmu + 1][NK], FP64 sums
+// of |k| and u32 mode counts [Nmu + 1][NK], the k-bin thresholds [NK + 2] --
+// must fit 220 KB: NK * (36 + 16 Nmu) + 8 <= 225280 bytes (NK <= 2048 up to
+// Nmu = 5, NK <= 1149 at Nmu = 10, NK <= 771 at Nmu = 16).
 #include "internal.h"
 #include "common.cuh"
 #include "binmath.cuh"
@@ -30,7 +37,7 @@ constexpr int kNaMaxNK = 2048;   // k bins
 constexpr int kNaMaxNmu = 16;    // wedges
 constexpr int kNaMaxW = kNaMaxNmu + 1;
 constexpr int kNaThreads = 256;
-constexpr int kNaChunkRows = 64;
+constexpr int kNaChunkRows = 256;  // rows per chunk of FP32 sums
 constexpr int kNaSegModes = 16;
 
 // scratch layout for the largest call (bytes, each part 256-aligned)
@@ -41,6 +48,12 @@ constexpr size_t kNaCnt = na_align(8ull * kNaMaxNK * kNaMaxW);          // u64 m
 constexpr size_t kNaThr = na_align(4ull * (kNaMaxNK + 2));              // u32 n^2 thresholds
 constexpr size_t kNaOut = na_align(8ull * kNaMaxNK * (6 + 3 * kNaMaxNmu));  // normalised outputs
 constexpr size_t kNoAllocScratchBytes = kNaPsum + kNaKsum + kNaCnt + kNaThr + kNaOut;  // 1.8 MB
+
+// shared accumulators of na_bin_kernel: NK * (36 + 16 Nmu) + 8 bytes
+constexpr size_t kNaSmemMax = 220 * 1024;
+constexpr size_t na_smem(int NK, int Nmu) {
+    return (size_t)NK * (4 * (4 + Nmu + 1) + 12 * (Nmu + 1)) + 4 * (size_t)(NK + 2);
+}
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -83,22 +96,21 @@ __global__ void na_thresholds_kernel(uint32_t *thr, int NK, double dKinv, uint32
 }
 
 // bins.cu's segment kernel (mode 1: P = |delta|^2 Vinv - Pshot) plus the
-// per-(bin, wedge) mode counts and sums of |k| (double-float sqrt per mode)
+// per-(bin, wedge) mode counts and sums of |k| (double-float sqrt per mode).
+// Shared memory holds FP32 power sums (added to the FP64 sums in the scratch
+// after every chunk of rows), FP64 sums of |k| and u32 counts (added to the
+// scratch once per CTA).
 __global__ void __launch_bounds__(kNaThreads)
 na_bin_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Pshot, const uint32_t *__restrict__ thr_g,
               double *__restrict__ gP, double *__restrict__ gK, unsigned long long *__restrict__ gN, int Ng_pad) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int NK = d.NK, W = d.W, NQ = 4 + W;
-    double *acc64 = reinterpret_cast<double *>(smem_raw);                    // [NQ][NK]
-    double *kacc = acc64 + (size_t)NK * NQ;                                  // [W][NK]
+    double *kacc = reinterpret_cast<double *>(smem_raw);                     // [W][NK]
     float *acc32 = reinterpret_cast<float *>(kacc + (size_t)NK * W);         // [NQ][NK]
     uint32_t *cnt = reinterpret_cast<uint32_t *>(acc32 + (size_t)NK * NQ);   // [W][NK]
     uint32_t *thr = cnt + (size_t)NK * W;                                     // [NK + 2]
     const int tid = threadIdx.x;
-    for (int e = tid; e < NK * NQ; e += blockDim.x) {
-        acc64[e] = 0;
-        acc32[e] = 0.f;
-    }
+    for (int e = tid; e < NK * NQ; e += blockDim.x) acc32[e] = 0.f;
     for (int e = tid; e < NK * W; e += blockDim.x) {
         kacc[e] = 0;
         cnt[e] = 0;
@@ -185,14 +197,14 @@ na_bin_kernel(BinDev d, const float *__restrict__ f, float Vinv, float Pshot, co
             }
         }
         __syncthreads();
+        // the chunk's FP32 sums into the FP64 sums of the scratch
         for (int e = tid; e < NK * NQ; e += blockDim.x) {
-            acc64[e] += (double)acc32[e];
+            const float v = acc32[e];
+            if (v != 0.f) atomicAdd(&gP[e], (double)v);
             acc32[e] = 0.f;
         }
         __syncthreads();
     }
-    for (int e = tid; e < NK * NQ; e += blockDim.x)
-        if (acc64[e] != 0) atomicAdd(&gP[e], acc64[e]);
     for (int e = tid; e < NK * W; e += blockDim.x) {
         if (kacc[e] != 0) atomicAdd(&gK[e], kacc[e]);
         if (cnt[e] != 0) atomicAdd(&gN[e], (unsigned long long)cnt[e]);
@@ -256,10 +268,12 @@ static int noalloc_run(const float *fk, int Ng, double L, double V, long Np, con
     const uint32_t h = Ng / 2, n2max = 3u * h * h;
     if ((int)floor(sqrt((double)n2max) * s.dKinv) >= NK)
         return set_error(ERR_RANGE, "a mode falls beyond the last of NK=%d k bins", NK);
-    const size_t smem = (size_t)NK * NQ * 12 + (size_t)NK * W * 12 + 4 * (size_t)(NK + 2);
-    if (smem > 220 * 1024)
-        return set_error(ERR_UNSUPPORTED, "fftgal_power_bins_noalloc: %d bins x %d wedges exceed shared memory", NK,
-                         Nmu);
+    const size_t smem = na_smem(NK, Nmu);
+    if (smem > kNaSmemMax)
+        return set_error(ERR_UNSUPPORTED,
+                         "fftgal_power_bins_noalloc: NK = %d k bins x Nmu = %d wedges need %zu bytes of shared "
+                         "accumulators, more than %zu (NK * (36 + 16 Nmu) + 8)",
+                         NK, Nmu, smem, kNaSmemMax);
     void *base = nullptr;
     FG_TRY(noalloc_scratch(&base));
     unsigned char *p = static_cast<unsigned char *>(base);

@@ -76,9 +76,13 @@ int fftgal_nk(int Ng, double L, double dK);
  *   los       line of sight (normalised internally, not modified)
  * Outputs (host, any may be NULL): K[NK], N[NK], Pl[NK*4] (l=0,2,4,6);
  * Kmu[NK*Nmu], Nmu_count[NK*Nmu], Pmu[NK*Nmu].  Bins are normalised exactly as
- * Pl()/Pmu() normalise them (empty multipole bins are NaN).  The grid is left
- * holding the deconvolved density field in k space (as after fft_p2k).
- * Requires an FP32 grid. */
+ * Pl()/Pmu() normalise them (empty multipole bins are NaN).  With the sync
+ * host view the grid is left holding the deconvolved density field in k space
+ * (as after fft_p2k, grid->f and the device grid); with the lazy view the
+ * finished field is binned without being stored (4.3 GB fewer writes at
+ * Ng = 1024) and the device grid's contents are unspecified until the next
+ * paint, import or copy.  The same holds for fftgal_power_batch_f32 and
+ * fftgal_power_rsd_f32.  Requires an FP32 grid. */
 int fftgal_power_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
                      double V, int where, const double los[3], double dK, int Nmu,
                      double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
@@ -138,8 +142,8 @@ int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const f
  * src/power.c:12-178).  Half the paint and FFT work of the interlaced call;
  * aliasing is not suppressed.  With the sync host view the grid then holds
  * the deconvolved field (grid->f and the device grid); with the lazy view the
- * device grid keeps the r2c output before deconvolution, which is applied
- * only while binning. */
+ * deconvolution is applied only while binning and the device grid's contents
+ * are unspecified until the next paint, import or copy. */
 int fftgal_power_single_f32(fft_t *grid, const float *x, const float *y, const float *z, long Np,
                             double V, int where, const double los[3], double dK, int Nmu,
                             double *K, long *N, double *Pl, double *Kmu, long *Nmu_count,
@@ -187,6 +191,15 @@ double fftgal_alias_envelope(double u);
 int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms[3]);
 /* measure now (clears the grid) and keep the fastest shapes on this grid */
 int fftgal_plan_autotune(fft_t *grid, double ms[3]);
+/* Forward FP32 transforms run their first two passes (r2c along k, then j)
+ * slab by slab: `planes` i planes of both interlacing grids per slab (a single
+ * grid takes twice as many), so that the j pass reads the k pass's output from
+ * L2 instead of HBM.  The default fills about half the L2 cache (8 planes at
+ * Ng = 1024 on GB300; 0 when a whole grid fits).  planes >= 0 sets it (0: no
+ * slabs, the k pass over the whole grid, then the j pass), -1 only queries;
+ * returns the value in use.  Results are bit-identical for every value (the
+ * same kernels transform the same rows and columns). */
+int fftgal_fft_slab_planes(fft_t *grid, int planes);
 /* in-place unnormalised FFTs of length N (a power of two from 4 to 2048) along
  * strided columns of complex FP32 data in GPU memory, with the kernels of the
  * grid's j and i passes: element n of column c (c < ncols) of batch b
@@ -271,7 +284,8 @@ long fftgal_device_bytes(fft_t *grid);
  * allocating library routine.
  *   fk         Ng*Ng*(Ng/2+1) complex FP32 values in the layout of the
  *              canonical grid (rows of Ng+2 floats), e.g. fftgal_device_grid()
- *              after fftgal_power_f32 or fft_p2k on an FP32 grid
+ *              after fft_p2k on an FP32 grid (or after fftgal_power_f32 with
+ *              the sync host view)
  *   V, Np      P = |fk|^2 / V - V / Np (src/power.c:55)
  *   los, dK, Nmu, outputs: as fftgal_power_f32 (outputs on the host)
  *   stream     cudaStream_t to run on (NULL: the legacy default stream); the
@@ -280,12 +294,18 @@ long fftgal_device_bytes(fft_t *grid);
  * shared by all calls: it holds the k-bin limits, per-bin sums and counts of
  * the last call and is cleared at the start of each.  Calls whose GPU work
  * overlaps (from several host threads, or on several streams) race on it.
+ * The call waits for `stream` (cudaStreamSynchronize) and copies the tables
+ * to the caller's host arrays before it returns.
  * Limits: NK <= 2048 k bins, 1 <= Nmu <= 16, Ng <= 4096, and the per-block
- * accumulators (about 12 * NK * (2*Nmu + 6) bytes) within 220 KB of shared
- * memory; larger requests return FFTGAL_ERR_RANGE / FFTGAL_ERR_UNSUPPORTED.
+ * shared accumulators NK * (36 + 16 * Nmu) + 8 <= 225280 bytes (220 KB):
+ * NK <= 2048 up to Nmu = 5, NK <= 1149 at Nmu = 10, NK <= 771 at Nmu = 16
+ * (Ng = 1024 with dK = 2 pi / L has NK = 887).  Larger requests return
+ * FFTGAL_ERR_RANGE (NK) or FFTGAL_ERR_UNSUPPORTED (shared memory).
  * The first call on each device looks up the scratch's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. */
+ * (cudaGetSymbolAddress) with that device current and keeps it for the life
+ * of the process; make that first call before any stream capture.  A
+ * cudaDeviceReset of that device after its first call is not supported (the
+ * kept address would be stale). */
 int fftgal_power_bins_noalloc(const float *fk, int Ng, double L, double V, long Np,
                               const double los[3], double dK, int Nmu, double *K,
                               long *N, double *Pl, double *Kmu, long *Nmu_count,

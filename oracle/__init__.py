@@ -36,14 +36,25 @@ _lp = C.POINTER(C.c_long)
 
 def build(ref: bool = False) -> None:
     """Compile liboracle.so (and the reference build when ``ref`` and the
-    reference sources exist)."""
-    targets = ["all"]
-    if ref and os.path.isdir(os.environ.get("FFTGAL_REFERENCE_DIR", "/root/reference")):
-        targets.append("ref")
-    env = dict(os.environ)
-    if "FFTGAL_REFERENCE_DIR" in os.environ:
-        env["REF"] = os.environ["FFTGAL_REFERENCE_DIR"]
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True, env=env)
+    reference sources exist: FFTGAL_REFERENCE_DIR, else the location the
+    build recipe oracle/Makefile names)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref and subprocess.run(["make", "-s", "-C", HERE, "have-ref"], capture_output=True).returncode == 0:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def reference_dir() -> str | None:
+    """The reference checkout: FFTGAL_REFERENCE_DIR, else the one the
+    reference build in oracle/_ref was compiled from, else None."""
+    d = os.environ.get("FFTGAL_REFERENCE_DIR")
+    if d:
+        return d if os.path.isdir(d) else None
+    try:
+        with open(os.path.join(HERE, "_ref", "SOURCE_DIR")) as fh:
+            d = fh.read().strip()
+    except OSError:
+        return None
+    return d if os.path.isdir(d) else None
 
 
 def _ptr(a: np.ndarray | None):

@@ -1,7 +1,7 @@
 """Write tests/golden/drivers_small.npz from the reference's OWN drivers.
 
-Run where the reference sources are present (default /root/reference,
-override with FFTGAL_REFERENCE_DIR):
+Run where the reference sources are present (oracle.reference_dir():
+FFTGAL_REFERENCE_DIR, or the checkout oracle/Makefile builds from):
 
     make -C oracle ref && python tests/golden/make_drivers_golden.py
 

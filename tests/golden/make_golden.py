@@ -1,7 +1,8 @@
 """Write the golden fixtures under tests/golden/ from the reference's OWN code.
 
-Run in a checkout where the reference sources are present (default
-/root/reference, override with FFTGAL_REFERENCE_DIR):
+Run in a checkout where the reference sources are present
+(oracle.reference_dir(): FFTGAL_REFERENCE_DIR, or the checkout oracle/Makefile
+builds from):
 
     make -C oracle ref && python tests/golden/make_golden.py
 

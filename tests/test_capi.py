@@ -5,12 +5,16 @@ import os
 import re
 import shutil
 import subprocess
+import sys
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF = os.environ.get("FFTGAL_REFERENCE_DIR", "/root/reference")
+sys.path.insert(0, ROOT)
+import oracle  # noqa: E402  (locates the reference checkout; test infrastructure)
+
+REF = oracle.reference_dir() or ""
 
 
 @pytest.fixture(scope="module")

@@ -94,7 +94,7 @@ def test_fft_matches_numpy(fg, prec, Ng):
 # ---------------------------------------------------------------------------
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 @pytest.mark.parametrize("Ng", [2, 3, 4, 5, 6, 8, 12, 16])
-def test_small_cases_match_reference(fg, oracle_lib, small, prec, Ng):
+def test_small_cases_match_reference(fg, oracle_lib, small, prec, Ng, tmp_path):
     key = f"ng{Ng}"
     L = float(small[key + "_L"])
     x, y, z = small[key + "_pos"]
@@ -127,8 +127,7 @@ def test_small_cases_match_reference(fg, oracle_lib, small, prec, Ng):
     Pshot = V / len(x)
     for il, los in enumerate(small["los_set"]):
         for idk, dK in enumerate((KF, 0.7 * KF, 2.5 * KF)):
-            fpl = f"/tmp/fftgal_test_pl_{os.getpid()}.txt"
-            fmu = f"/tmp/fftgal_test_pmu_{os.getpid()}.txt"
+            fpl, fmu = str(tmp_path / "pl.txt"), str(tmp_path / "pmu.txt")
             losh = g.pl(cat, los, dK, fpl)
             g.pmu(cat, los, dK, fmu)
             got = fg.read_table(fpl)
