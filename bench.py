@@ -301,9 +301,9 @@ def algorithmic_bytes(Ng: int, Np: int):
     R4 = Ng ** 3 * 4                           # one unpadded real grid
     return {
         "upload": 12 * Np,
-        "paint_key": 12 * Np + 8 * Np,         # read x,y,z; write key + rank
+        "paint_key": 12 * Np,                  # read x,y,z (key histogram in L2)
         "paint_scan": 0,
-        "paint_scatter": 12 * Np + 8 * Np + 16 * Np,
+        "paint_scatter": 12 * Np + 16 * Np,    # read x,y,z; write the 16-byte records
         "paint_tile": 16 * Np + 2 * G4,        # sorted records in, both grids out
         "fft_k": 2 * (R4 + G4),                # both grids, read real rows, write half spectra
         "fft_j": 2 * 2 * G4,
@@ -470,8 +470,12 @@ def run_ours(args):
                              f"positions widened to FP64): FP64 oracle restating src/fft.c + src/power.c, "
                              f"fft_p2k+P+Pl+Pmu, {secs:.1f} s on 1 core"}
         par = parity_block(res, Ng, Np, args.mock, live)
-        par["e2e_matches_device_resident"] = bool(
-            np.array_equal(res_e2e[-1]["P"], res["P"]) and np.array_equal(res_e2e[-1]["Pmu"], res["Pmu"]))
+        # the same catalog through the e2e call: equal up to the order of the
+        # FP64 atomic additions of the bin sums
+        den = np.abs(res["P"][:, :1]) + L_BOX ** 3 / Np
+        fin = np.isfinite(res["P"])
+        par["e2e_vs_device_resident_max_rel"] = float(
+            (np.abs(res_e2e[-1]["P"] - res["P"]) / den)[fin].max())
         out = {
             "metric": METRIC, "value": value, "unit": "catalogs/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,

@@ -108,7 +108,6 @@ SIGNATURES = {
     "fftgal_alias_envelope": (C.c_double, [C.c_double]),
     "fftgal_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
     "fftgal_plan_autotune": (C.c_int, [C.c_void_p, _dp]),
-    "fftgal_fft_slab_planes": (C.c_int, [C.c_void_p, C.c_int]),
     "fftgal_plan_lookup": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "fftgal_plan_store": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), _dp,
                                     C.c_char_p]),
@@ -342,14 +341,6 @@ class Grid:
         ms = np.zeros(3)
         _check(lib().fftgal_plan_autotune(self.p, ms.ctypes.data_as(_dp)))
         return ms
-
-    def slab_planes(self, planes: int = -1) -> int:
-        """i planes per slab of the forward k + j passes (fftgal_fft_slab_planes):
-        planes >= 0 sets it, -1 queries; returns the value in use."""
-        r = lib().fftgal_fft_slab_planes(self.p, int(planes))
-        if r < 0:
-            _check(r)
-        return r
 
     def set_stream(self, stream_ptr: int | None):
         """Run the grid's work on a CUDA stream: None for the library's own

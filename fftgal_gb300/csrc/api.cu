@@ -233,7 +233,7 @@ static int leave(fft_t *self, bool modified) {
     if (modified) ++g->version;
     if (g->view == FFTGAL_VIEW_SYNC && modified) FG_TRY(device_to_host(g, self->f, g->pinned));
     FG_CUDA(cudaStreamSynchronize(g->stream));
-    return OK;
+    return fft2_tma_check();
 }
 
 // ---- helpers ------------------------------------------------------------------------------
@@ -919,18 +919,6 @@ extern "C" int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms
     return OK;
 }
 
-extern "C" int fftgal_fft_slab_planes(fft_t *grid, int planes) {
-    if (!grid) return set_error(ERR_ARG, "null grid");
-    Grid *g = G(grid);
-    if (planes >= 0) {
-        if (planes > 0 && !fft2_supported(grid->Ng, g->prec))
-            return set_error(ERR_UNSUPPORTED, "slabs need the two-level FP32 kernels (power-of-two Ng, FP32 grid)");
-        g->fft.kj_planes = planes;
-        ++g->version;
-    }
-    return g->fft.kj_planes;
-}
-
 extern "C" int fftgal_plan_autotune(fft_t *grid, double ms[3]) {
     if (!grid) return set_error(ERR_ARG, "null grid");
     Grid *g = G(grid);
@@ -968,6 +956,9 @@ extern "C" int fftgal_copy_grid(fft_t *grid, void *buf, int to_grid) {
     } else {
         FG_CUDA(cudaMemcpy(buf, g->d_f, bytes, cudaMemcpyDefault));
     }
+    // a device-to-device cudaMemcpy returns before the copy is done, and the
+    // grid's non-blocking stream does not wait for the legacy stream
+    FG_CUDA(cudaStreamSynchronize(cudaStreamLegacy));
     return OK;
 }
 
@@ -1066,15 +1057,9 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
     FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, ngr, st, tm ? ev + 2 : nullptr,
                  vel ? &rsd : nullptr));
     void *grids[2] = {g->d_f, g->d_aux};
-    // k and j passes slab by slab (the fft_k stage then times both, fft_j is empty)
-    if (g->fft.kj_planes > 0) {
-        FG_TRY(fft_pass_kj(&g->fft, grids, ngr, st));
-        if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
-    } else {
-        FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
-        if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
-        FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
-    }
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
+    if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
+    FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
     FG_TRY(fft_pass_i(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
@@ -1111,6 +1096,7 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
         FG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[kStages]));
         g->stage_ms[kStages] = ms;
     }
+    FG_TRY(fft2_tma_check());  // the binning's read-back synchronised the stream
     FG_TRY(finish_pl(geo, Psum, K, N, Plout));
     FG_TRY(finish_pmu(geo, Pw, Kmu, Nmu_count, Pmuout));
     if (g->view == FFTGAL_VIEW_SYNC) FG_TRY(device_to_host(g, grid->f, g->pinned));
@@ -1231,7 +1217,8 @@ static int enqueue_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cud
     FG_TRY(paint(&g->tiling, &g->scratch, 4, d, d + capNp, d + 2 * capNp, 4, capNp, Ng / grid->L, spec, 2, st,
                  nullptr, nullptr, g->d_scal + b));
     void *grids[2] = {g->d_f, g->d_aux};
-    FG_TRY(fft_pass_kj(&g->fft, grids, 2, st));
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
+    FG_TRY(fft_pass_j(&g->fft, grids, 2, -1, st));
     FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
     BinFinish fin;
     fin.A = g->d_f;
@@ -1342,8 +1329,8 @@ static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const
     }
     // recapture whenever a buffer, table, plan or bin layout the graphs name changed
     std::vector<uint64_t> key;
-    const void *ptrs[] = {g->d_batch[0], g->d_batch[1], g->d_f,         g->d_aux,           g->scratch.key,
-                          g->scratch.rank, g->scratch.sorted, g->scratch.hist, g->scratch.scan_tmp, geo,
+    const void *ptrs[] = {g->d_batch[0], g->d_batch[1], g->d_f,         g->d_aux,           g->scratch.cursor,
+                          g->scratch.sorted, g->scratch.hist, g->scratch.scan_tmp, geo,
                           geo->d_acc,      geo->d_thr,        g->d_tab,       g->d_scal};
     for (const void *q : ptrs) key_push(key, (uintptr_t)q);
     key_push(key, capNp);
@@ -1395,6 +1382,7 @@ static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const
     }
     FG_CUDA(cudaStreamSynchronize(g->stream));
     FG_CUDA(cudaStreamSynchronize(g->copy_stream));
+    FG_TRY(fft2_tma_check());
     for (int a = 0; a < 3; ++a) grid->offset[a] = 0;
     ++g->version;
     const int NK = spec.NK;

@@ -486,10 +486,6 @@ int fft_plan_create(FftPlan *p, int Ng, int prec) {
     FG_TRY(choose_shape(p->axis, prec, cmax, 0, 0, &p->cols, &p->col_threads, &p->col_smem));
     const Fft1dPlan &kp = p->even ? p->half : p->axis;
     FG_TRY(choose_shape(kp, prec, cmax, 1, 1, &p->rows, &p->row_threads, &p->row_smem));
-    // slabs of the forward k + j passes (FP32 two-level kernels only);
-    // FFTGAL_KJ_PLANES overrides the L2-sized default (0: no slabs)
-    p->kj_planes = fft2_supported(Ng, prec) ? fft_kj_default_planes(Ng, 2) : 0;
-    if (const char *e = getenv("FFTGAL_KJ_PLANES")) p->kj_planes = atoi(e) > 0 ? atoi(e) : 0;
     return OK;
 }
 
@@ -572,42 +568,14 @@ int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaS
 }
 
 int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s) {
+    if (fft2_tma_supported(p->Ng, p->prec))
+        return fft2_cols_tma(p->Ng, p->axis.tw, grids[0], ngrids > 1 ? grids[1] : grids[0], ngrids, sign, s);
     return cols_pass(p, grids, ngrids, sign, (long)p->Ng * p->nh, p->nh, s, p->tune[2]);
 }
 
-int fft_kj_default_planes(int Ng, int ngrids) {
-    int dev = 0, l2 = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
-        return 0;
-    const long plane = (long)Ng * 2 * (Ng / 2 + 1) * 4 * (ngrids > 0 ? ngrids : 1);
-    const long budget = (long)l2 / 2;
-    if ((long)Ng * plane <= budget) return 0;
-    const long P = budget / plane;
-    return P < 1 ? 1 : (int)P;
-}
-
-int fft_pass_kj(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s) {
-    // kj_planes counts planes of two grids: a single grid takes twice as many
-    const int Ng = p->Ng, P = ngrids > 1 ? p->kj_planes : 2 * p->kj_planes;
-    if (P <= 0 || P >= Ng || !fft2_supported(Ng, p->prec)) {
-        FG_TRY(fft_pass_k_r2c(p, grids, ngrids, s));
-        return fft_pass_j(p, grids, ngrids, -1, s);
-    }
-    void *g1 = ngrids > 1 ? grids[1] : grids[0];
-    const long plane_c = (long)Ng * p->nh;  // complex values per i plane
-    for (int i0 = 0; i0 < Ng; i0 += P) {
-        const int np = Ng - i0 < P ? Ng - i0 : P;
-        FG_TRY(fft2_k_r2c(Ng, p->half.tw, p->rtw, grids[0], g1, ngrids, s, p->tune[0], (long)i0 * Ng,
-                          (long)np * Ng));
-        float2 *a = static_cast<float2 *>(grids[0]) + i0 * plane_c;
-        float2 *b = static_cast<float2 *>(g1) + i0 * plane_c;
-        FG_TRY(fft2_cols(Ng, p->axis.tw, a, b, ngrids, p->nh, p->nh, plane_c, np, -1, s, p->tune[1]));
-    }
-    return OK;
-}
-
 int fft_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s) {
-    FG_TRY(fft_pass_kj(p, grids, ngrids, s));
+    FG_TRY(fft_pass_k_r2c(p, grids, ngrids, s));
+    FG_TRY(fft_pass_j(p, grids, ngrids, -1, s));
     FG_TRY(fft_pass_i(p, grids, ngrids, -1, s));
     return OK;
 }

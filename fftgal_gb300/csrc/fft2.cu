@@ -19,7 +19,11 @@
 #include "internal.h"
 #include "common.cuh"
 
+#include <cuda.h>  // CUtensorMap and its encode function's types; the function comes from the driver at run time
+
 #include <math.h>
+#include <stdlib.h>
+#include <mutex>
 
 namespace fg {
 
@@ -253,6 +257,185 @@ fft2_k_r2c_kernel(float *g0, float *g1, long nrows, int Ng_pad, int R,
     }
 }
 
+// ---- widely strided axis (the i pass), columns staged by TMA ----------------------------------
+// Ng = 512 or 1024 = 32 x N2.  A tile is C = 8 adjacent complex columns at one
+// (grid, j) over all Ng rows i: Ng rows of 64 bytes, brought into shared
+// memory by cp.async.bulk.tensor (boxes of 256 rows) with an mbarrier per
+// stage.  The tensor map views one i plane as a row of Ng * Ng_pad floats and
+// the planes as its rows (stride Ng Ng_pad floats, a multiple of 16 bytes);
+// a tile starts at float j Ng_pad + 2 kc0 with kc0 = 8 m + (j & 1), which is
+// a multiple of 4 floats (16 bytes) for every j (Ng_pad = 2 mod 4).  The
+// column each j leaves (kc = Ng/2 for even j, kc = 0 for odd j) is
+// transformed by fft2_cols_kernel.
+// Persistent, one CTA per SM, three 64 KB stages and two groups of 256
+// threads: group (l & 1) transforms the CTA's l-th tile while the loads of the
+// next tiles are in flight; as soon as a group has read its stage into
+// registers, it issues the load of tile l + 3 into that stage.  Step 1 (a
+// 32-point FFT per (column, n2), twiddle) works in place in the stage, step 2
+// (an N2-point FFT per (column, k1)) reads it into registers and stores the
+// results to HBM.  Every mbarrier wait is bounded: on a time-out the kernel
+// sets *err, stops issuing, waits (bounded) for its loads in flight and returns.
+constexpr int kTmaCols = 8;
+constexpr int kTmaStages = 3;
+constexpr int kTmaThreads = 512;   // two groups of 256
+constexpr int kTmaBoxRows = 256;
+constexpr unsigned kTmaPollLimit = 1u << 24;  // polls of ~32 ns: about half a second
+
+__device__ int g_tma_err;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// true once the phase with the given parity has completed; false after the poll limit
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (unsigned it = 0; it < kTmaPollLimit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        __nanosleep(32);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void group_sync(int grp) {
+    asm volatile("bar.sync %0, 256;" ::"r"(1 + grp) : "memory");
+}
+
+template <int N2>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+fft2_cols_tma_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                     float2 *g0, float2 *g1, int ngrids, int Ng, int nh, int Ng_pad, long es,
+                     const float2 *__restrict__ W, int sign) {
+    constexpr int N1 = 32, N = N1 * N2, C = kTmaCols;
+    constexpr uint32_t kTileBytes = N * C * sizeof(float2);
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    float2 *stages = reinterpret_cast<float2 *>(smem_raw);  // [kTmaStages][N][C]
+    __shared__ __align__(8) uint64_t full[kTmaStages];
+    // issued[s]: the last local tile armed on stage s (written after the
+    // previous use of the stage completed); consumed[s]: the last one read
+    __shared__ volatile long issued[kTmaStages], consumed[kTmaStages];
+    __shared__ volatile int group_abort[2];
+
+    const int ntj = (nh - 1) / C;  // tiles per (grid, j)
+    const long ntiles = (long)ngrids * Ng * ntj;
+    const long nloc = ntiles > (long)blockIdx.x ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const int t = threadIdx.x, grp = t >> 8, gt = t & 255;
+
+    auto tile_of = [&](long l, int &g, int &j, int &kc0) {
+        const long q = blockIdx.x + (long)gridDim.x * l;
+        g = (int)(q / ((long)Ng * ntj));
+        const long r = q - (long)g * Ng * ntj;
+        j = (int)(r / ntj);
+        kc0 = C * (int)(r - (long)j * ntj) + (j & 1);
+    };
+    // one thread: arm stage l % 3 and issue the loads of local tile l
+    auto issue = [&](long l) {
+        int g, j, kc0;
+        tile_of(l, g, j, kc0);
+        const int s = (int)(l % kTmaStages);
+        float2 *dst = stages + (size_t)s * N * C;
+        mbar_expect_tx(&full[s], kTileBytes);
+        const CUtensorMap *tm = g ? &tm1 : &tm0;
+        const int x = j * Ng_pad + 2 * kc0;
+#pragma unroll
+        for (int y = 0; y < N; y += kTmaBoxRows) tma_load_2d(dst + (size_t)y * C, tm, x, y, &full[s]);
+        __threadfence_block();
+        issued[s] = l;
+    };
+    if (t == 0) {
+        for (int s = 0; s < kTmaStages; ++s) {
+            mbar_init(&full[s], 1);
+            issued[s] = consumed[s] = -1;
+        }
+        group_abort[0] = group_abort[1] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (t == 0)
+        for (long l = 0; l < kTmaStages && l < nloc; ++l) issue(l);
+
+    for (long l = grp; l < nloc; l += 2) {
+        const int s = (int)(l % kTmaStages);
+        // the parity test below is only meaningful once the stage's previous
+        // phase has completed, which its issuer waited for before arming tile l
+        bool armed = false;
+        for (unsigned it = 0; it < kTmaPollLimit && !armed; ++it) {
+            armed = issued[s] >= l;
+            if (!armed) __nanosleep(32);
+        }
+        if (!armed || !mbar_wait(&full[s], (uint32_t)((l / kTmaStages) & 1))) {
+            atomicExch(&g_tma_err, 1);
+            group_abort[grp] = 1;
+        }
+        group_sync(grp);
+        if (group_abort[grp]) break;  // the group leaves together (the flag is only ever set)
+        int g, j, kc0;
+        tile_of(l, g, j, kc0);
+        float2 *S = stages + (size_t)s * N * C;
+        if (gt < C * N2) {  // step 1: x[N2 n1 + n2] -> Y[k1, n2] W_N^(n2 k1), in place
+            const int c = gt & (C - 1), n2 = gt >> 3;
+            float2 v[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; ++n1) v[n1] = S[(N2 * n1 + n2) * C + c];
+            reg_fft<N1>(v, sign);
+#pragma unroll
+            for (int k1 = 1; k1 < N1; ++k1)
+                if (n2) v[k1] = cmul(v[k1], twid(W, n2 * k1, sign));
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) S[(N2 * k1 + n2) * C + c] = v[k1];
+        }
+        group_sync(grp);
+        // step 2: one (column, k1) per thread; odd k1 read each pair of rows in
+        // swapped order so that a warp's 4 rows fall in both halves of the banks
+        const int c = gt & (C - 1), k1 = gt >> 3;
+        const bool odd = k1 & 1;
+        float2 u[N2];
+#pragma unroll
+        for (int m = 0; m < N2; m += 2) {
+            const float2 a = S[(N2 * k1 + m + (odd ? 1 : 0)) * C + c];
+            const float2 b = S[(N2 * k1 + m + (odd ? 0 : 1)) * C + c];
+            u[m] = odd ? b : a;
+            u[m + 1] = odd ? a : b;
+        }
+        group_sync(grp);
+        if (gt == 0) {
+            consumed[s] = l;
+            if (l + kTmaStages < nloc) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(l + kTmaStages);
+            }
+        }
+        reg_fft<N2>(u, sign);
+        float2 *base = (g ? g1 : g0) + (long)j * nh + kc0 + c;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; ++k2) base[(long)(k1 + N1 * k2) * es] = u[k2];
+    }
+    __syncthreads();
+    if (t == 0)  // loads still in flight after a time-out land before the CTA exits
+        for (int s = 0; s < kTmaStages; ++s)
+            if (issued[s] > consumed[s]) mbar_wait(&full[s], (uint32_t)((issued[s] / kTmaStages) & 1));
+}
+
 // ---- host side ----------------------------------------------------------------------------
 
 static bool g_w32_ready = false;
@@ -359,6 +542,94 @@ int fft2_default_shape(int Ng, int which) {
 
 int fft2_prepare() { return ensure_w32(); }
 
+// ---- TMA-staged i pass ------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int tensor_map_encoder(EncodeTiledFn *fn) {
+    static std::mutex m;
+    static EncodeTiledFn enc = nullptr;
+    std::lock_guard<std::mutex> lock(m);
+    if (!enc) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+            return set_error(ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
+        enc = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    *fn = enc;
+    return OK;
+}
+
+// one FP32 grid as [Ng planes i][Ng * Ng_pad floats], boxes of 16 floats x 256 planes
+static int plane_tensor_map(CUtensorMap *tm, void *grid, int Ng) {
+    EncodeTiledFn enc;
+    FG_TRY(tensor_map_encoder(&enc));
+    const cuuint64_t Ng_pad = 2 * (cuuint64_t)(Ng / 2 + 1);
+    const cuuint64_t dims[2] = {(cuuint64_t)Ng * Ng_pad, (cuuint64_t)Ng};
+    const cuuint64_t strides[1] = {(cuuint64_t)Ng * Ng_pad * sizeof(float)};
+    const cuuint32_t box[2] = {2 * kTmaCols, (cuuint32_t)(Ng < kTmaBoxRows ? Ng : kTmaBoxRows)};
+    const cuuint32_t estr[2] = {1, 1};
+    if (reinterpret_cast<uintptr_t>(grid) % 16 || strides[0] % 16)
+        return set_error(ERR_UNSUPPORTED, "TMA i pass: grid address or plane stride not 16-byte aligned");
+    const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, grid, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return OK;
+}
+
+bool fft2_tma_supported(int Ng, int prec) {
+    static const int off = [] {
+        const char *e = getenv("FFTGAL_TMA");
+        return e && e[0] == '0';
+    }();
+    return !off && prec == 4 && (Ng == 512 || Ng == 1024);
+}
+
+int fft2_cols_tma(int Ng, const void *W, void *g0, void *g1, int ngrids, int sign, cudaStream_t s) {
+    FG_TRY(ensure_w32());
+    if (!fft2_tma_supported(Ng, 4)) return set_error(ERR_UNSUPPORTED, "TMA i pass: Ng=%d", Ng);
+    const int nh = Ng / 2 + 1, Ng_pad = 2 * nh;
+    const long es = (long)Ng * nh;  // complex values between consecutive i
+    void *b = ngrids > 1 ? g1 : g0;
+    CUtensorMap tm[2];
+    FG_TRY(plane_tensor_map(&tm[0], g0, Ng));
+    FG_TRY(plane_tensor_map(&tm[1], b, Ng));
+    const size_t smem = (size_t)kTmaStages * Ng * kTmaCols * sizeof(float2);
+    const long ntiles = (long)ngrids * Ng * ((nh - 1) / kTmaCols);
+    const unsigned nb = (unsigned)(ntiles < num_sms() ? ntiles : num_sms());
+    if (Ng == 1024) {
+        FG_CUDA(cudaFuncSetAttribute(fft2_cols_tma_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fft2_cols_tma_kernel<32><<<nb, kTmaThreads, smem, s>>>(tm[0], tm[1], (float2 *)g0, (float2 *)b, ngrids, Ng,
+                                                               nh, Ng_pad, es, (const float2 *)W, sign);
+    } else {
+        FG_CUDA(cudaFuncSetAttribute(fft2_cols_tma_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fft2_cols_tma_kernel<16><<<nb, kTmaThreads, smem, s>>>(tm[0], tm[1], (float2 *)g0, (float2 *)b, ngrids, Ng,
+                                                               nh, Ng_pad, es, (const float2 *)W, sign);
+    }
+    FG_LAUNCHED(1);
+    // the column each j leaves to fft2_cols_kernel: kc = Ng/2 at even j, kc = 0 at odd j
+    float2 *a2 = static_cast<float2 *>(g0), *b2 = static_cast<float2 *>(b);
+    const int lc = Ng == 512 ? 1 : 0;  // at least 32 threads per CTA
+    FG_TRY(fft2_cols(Ng, W, a2 + Ng / 2, b2 + Ng / 2, ngrids, 1, es, 2L * nh, Ng / 2, sign, s, lc));
+    FG_TRY(fft2_cols(Ng, W, a2 + nh, b2 + nh, ngrids, 1, es, 2L * nh, Ng / 2, sign, s, lc));
+    return OK;
+}
+
+int fft2_tma_check() {
+    int v = 0;
+    FG_CUDA(cudaMemcpyFromSymbol(&v, g_tma_err, sizeof(int)));
+    if (v) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_tma_err, &zero, sizeof(int));
+        return set_error(ERR_CUDA, "TMA column pass: a shared-memory stage never arrived (wait timed out)");
+    }
+    return OK;
+}
+
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
               long nbatch, int sign, cudaStream_t s, int logC_req) {
     FG_TRY(ensure_w32());
@@ -410,18 +681,13 @@ int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, l
         return OK;                                                                                         \
     }
 
-int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s, int R_req,
-               long row0, long nrows_req) {
+int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s, int R_req) {
     FG_TRY(ensure_w32());
     const int M = Ng / 2;
     int N1, N2;
     if (!split2(M, &N1, &N2)) return set_error(ERR_UNSUPPORTED, "fft2_k_r2c: Ng=%d", Ng);
     const int Ng_pad = 2 * (M + 1);
-    const long nrows = nrows_req >= 0 ? nrows_req : (long)Ng * Ng - row0;
-    if (row0 < 0 || nrows < 1 || row0 + nrows > (long)Ng * Ng)
-        return set_error(ERR_ARG, "fft2_k_r2c: rows [%ld, %ld) outside the grid", row0, row0 + nrows);
-    g0 = static_cast<float *>(g0) + row0 * Ng_pad;
-    g1 = static_cast<float *>(g1) + row0 * Ng_pad;
+    const long nrows = (long)Ng * Ng;
     int R = k_default_rows(N2);
     if (R_req > 0) {
         if (!fft2_valid_shape(Ng, 0, R_req))

@@ -73,11 +73,6 @@ struct FftPlan {
     // autotuner or a plan file: [0] k-pass rows per CTA (0 = built-in),
     // [1] j-pass and [2] i-pass log2 columns per CTA (-1 = built-in)
     int tune[3] = {0, -1, -1};
-    // forward r2c of FP32 grids: the k and j passes run on slabs of this many
-    // i planes (of two grids; a single grid takes twice as many), k pass then
-    // j pass per slab, so that the j pass finds the k pass's output in L2
-    // (0: one slab, the whole grid)
-    int kj_planes = 0;
 };
 
 int fft_plan_create(FftPlan *p, int Ng, int prec);
@@ -90,23 +85,24 @@ int fft_c2r(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_k_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
 int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
-// the forward k and j passes, slab by slab of p->kj_planes i planes
-int fft_pass_kj(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
-// i planes per slab of fft_pass_kj whose k-pass output of `ngrids` FP32
-// grids fits about half of the L2 cache (0: the whole grid fits)
-int fft_kj_default_planes(int Ng, int ngrids);
 // two-level FP32 kernels (fft2.cu) for power-of-two Ng in [4, 1024]
 bool fft2_supported(int Ng, int prec);
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
               long nbatch, int sign, cudaStream_t s, int logC_req = -1);
 int fft2_k_r2c(int Ng, const void *W, const void *rtw, void *g0, void *g1, int ngrids, cudaStream_t s,
-               int R_req = 0, long row0 = 0, long nrows = -1);
+               int R_req = 0);
 // launch shape `v` of pass `which` (0 = k rows per CTA, 1 = j / 2 = i log2
 // columns per CTA) is launchable for Ng; the built-in choice of each pass
 bool fft2_valid_shape(int Ng, int which, int v);
 int fft2_default_shape(int Ng, int which);
 // device twiddle tables of the two-level kernels (built once per device)
 int fft2_prepare();
+// TMA-staged strided pass along i of FP32 grids (Ng = 512 or 1024; FFTGAL_TMA=0
+// turns it off): the i pass of fft_pass_i; fft2_tma_check reports (and
+// clears) a time-out of its bounded mbarrier waits -- call it after a sync
+bool fft2_tma_supported(int Ng, int prec);
+int fft2_cols_tma(int Ng, const void *W, void *g0, void *g1, int ngrids, int sign, cudaStream_t s);
+int fft2_tma_check();
 // time every valid launch shape of the three r2c passes on `grid` (one FP32
 // grid of the plan's size; its contents are transformed in place) and keep the
 // fastest in p->tune; ms[3] = the chosen shapes' times
@@ -128,11 +124,10 @@ struct PaintTiling {
 
 struct PaintScratch {
     long cap_particles = 0;
-    uint32_t *key = nullptr;      // [cap] tile/class key of each particle
-    uint32_t *rank = nullptr;     // [cap] rank within its key
     void *sorted = nullptr;       // [cap] sorted records (float4 or double x3)
     long cap_keys = 0;
     uint32_t *hist = nullptr;     // [nkeys + 1] counts -> exclusive offsets
+    uint32_t *cursor = nullptr;   // [nkeys + 1] next free slot per key while scattering
     uint32_t *scan_tmp = nullptr; // block sums for the scan
     size_t bytes = 0;
 };

@@ -5,14 +5,18 @@
 // cubic B-spline weights of src/fft.c:83-88, cells wrapped mod Ng.  The GPU
 // organisation is new:
 //
-//  1. key     : every particle gets the key (tile, class) of its base cell.  The
+//  1. count   : every particle gets the key (tile, class) of its base cell.  The
 //               grid is cut into tiles of at most 16 x 16 x 32 cells (i, j, k);
 //               per axis the class says whether the particle's stencil (over
 //               all painted grids) reaches into the lower (1) or upper (2)
-//               neighbour tile, or neither (0).  The rank of the particle
-//               within its key comes from the histogram atomic.
-//  2. scan    : exclusive prefix sum of the key histogram.
-//  3. scatter : particles are written in key order.
+//               neighbour tile, or neither (0).  Only the key histogram is
+//               written (fire-and-forget atomics).
+//  2. scan    : exclusive prefix sum of the key histogram, copied to a cursor
+//               array.
+//  3. scatter : the key is formed again and each particle's record is written
+//               at the slot its key's cursor atomic returns.  The order within
+//               a key depends on the atomics' order; the FP32 paint sums in
+//               fixed point, so the painted grid does not.
 //  4. paint   : one CTA per tile owns its cells.  It pulls the particles of its
 //               own tile and only the boundary classes of its 26 neighbours,
 //               accumulates their weights in shared memory and writes every
@@ -203,8 +207,10 @@ template <> struct Rec<double> { struct type { double x, y, z; }; };
 
 // ---- 1. key + histogram -------------------------------------------------------
 
+// the key of a particle; for FP32 positions also its packed record words
+// (b0 << fb) | fraction per axis
 template <typename P>
-__device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintParams &pp) {
+__device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintParams &pp, uint32_t *rec = nullptr) {
     const int Ng = pp.Ng;
     int t[3], cls[3];
 #pragma unroll
@@ -213,6 +219,7 @@ __device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintPara
         uint32_t dq0 = 0;
         if constexpr (sizeof(P) == 4) {
             cell0(pos[a], pp.ax[a], Ng, pp.fb, b0, dq0);
+            if (rec) rec[a] = ((uint32_t)b0 << pp.fb) | dq0;
         } else {
             P d;
             coord(pos[a], pp.ax[a], 0, Ng, b0, d);
@@ -252,15 +259,12 @@ __device__ __forceinline__ uint32_t paint_key_of(const P pos[3], const PaintPara
 template <typename P>
 __global__ void paint_key_kernel(const P *__restrict__ x, const P *__restrict__ y,
                                  const P *__restrict__ z, long Np, PaintParams pp,
-                                 uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                                  uint32_t *__restrict__ hist, const DevScalars *__restrict__ ds) {
     if (ds) Np = ds->Np;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
         P pos[3] = {x[p], y[p], z[p]};
         rsd_displace(pp, p, pos);
-        const uint32_t k = paint_key_of<P>(pos, pp);
-        key[p] = k;
-        rank[p] = atomicAdd(&hist[k], 1u);
+        atomicAdd(&hist[paint_key_of<P>(pos, pp)], 1u);
     }
 }
 
@@ -357,33 +361,26 @@ static int exclusive_scan(uint32_t *a, long n, uint32_t *bsum, cudaStream_t st) 
 template <typename P>
 __global__ void paint_scatter_kernel(const P *__restrict__ x, const P *__restrict__ y,
                                      const P *__restrict__ z, long Np, PaintParams pp,
-                                     const uint32_t *__restrict__ key,
-                                     const uint32_t *__restrict__ rank,
-                                     const uint32_t *__restrict__ off,
+                                     uint32_t *__restrict__ cursor,
                                      typename Rec<P>::type *__restrict__ sorted,
                                      const DevScalars *__restrict__ ds) {
     if (ds) Np = ds->Np;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < Np; p += (long)gridDim.x * blockDim.x) {
-        const uint32_t dst = off[key[p]] + rank[p];
+        P pos[3] = {x[p], y[p], z[p]};
+        rsd_displace(pp, p, pos);
         typename Rec<P>::type r;
+        uint32_t k;
         if constexpr (sizeof(P) == 4) {
-            float pos[3] = {x[p], y[p], z[p]};
-            rsd_displace(pp, p, pos);
             uint32_t w[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                int b0;
-                uint32_t dq;
-                cell0(pos[a], pp.ax[a], pp.Ng, pp.fb, b0, dq);
-                w[a] = ((uint32_t)b0 << pp.fb) | dq;
-            }
+            k = paint_key_of<P>(pos, pp, w);
             r = make_uint4(w[0], w[1], w[2], 0u);
         } else {
-            r.x = x[p];
-            r.y = y[p];
-            r.z = z[p];
+            k = paint_key_of<P>(pos, pp);
+            r.x = pos[0];
+            r.y = pos[1];
+            r.z = pos[2];
         }
-        sorted[dst] = r;
+        sorted[atomicAdd(&cursor[k], 1u)] = r;
     }
 }
 
@@ -1009,36 +1006,32 @@ void paint_tiling_destroy(PaintTiling *t) {
 }
 
 void paint_scratch_free(PaintScratch *s) {
-    cudaFree(s->key);
-    cudaFree(s->rank);
     cudaFree(s->sorted);
     cudaFree(s->hist);
+    cudaFree(s->cursor);
     cudaFree(s->scan_tmp);
     *s = PaintScratch();
 }
 
 static int ensure_scratch(PaintScratch *s, long Np, long nkeys) {
     if (Np > s->cap_particles) {
-        cudaFree(s->key);
-        cudaFree(s->rank);
         cudaFree(s->sorted);
-        s->key = s->rank = nullptr;
         s->sorted = nullptr;
         const long cap = Np + Np / 8 + 1024;
-        FG_CUDA(cudaMalloc(&s->key, sizeof(uint32_t) * cap));
-        FG_CUDA(cudaMalloc(&s->rank, sizeof(uint32_t) * cap));
         FG_CUDA(cudaMalloc(&s->sorted, 32 * (size_t)cap));  // fits float4 and 3 doubles
         s->cap_particles = cap;
     }
     if (nkeys + 1 > s->cap_keys) {
         cudaFree(s->hist);
+        cudaFree(s->cursor);
         cudaFree(s->scan_tmp);
-        s->hist = s->scan_tmp = nullptr;
+        s->hist = s->cursor = s->scan_tmp = nullptr;
         FG_CUDA(cudaMalloc(&s->hist, sizeof(uint32_t) * (nkeys + 1)));
+        FG_CUDA(cudaMalloc(&s->cursor, sizeof(uint32_t) * (nkeys + 1)));
         FG_CUDA(cudaMalloc(&s->scan_tmp, sizeof(uint32_t) * (ceil_div(nkeys + 1, kScanBlock) + 1)));
         s->cap_keys = nkeys + 1;
     }
-    s->bytes = (sizeof(uint32_t) * 2 + 32) * (size_t)s->cap_particles + sizeof(uint32_t) * (size_t)s->cap_keys;
+    s->bytes = (size_t)32 * s->cap_particles + 2 * sizeof(uint32_t) * (size_t)s->cap_keys;
     return OK;
 }
 
@@ -1114,23 +1107,23 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (Np > 0) {
         if (pos_prec == 4)
             paint_key_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z, Np,
-                                                       pp, s->key, s->rank, s->hist, ds);
+                                                       pp, s->hist, ds);
         else
             paint_key_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y, (const double *)z,
-                                                        Np, pp, s->key, s->rank, s->hist, nullptr);
+                                                        Np, pp, s->hist, nullptr);
         FG_LAUNCHED(1);
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[0], st));
     FG_TRY(exclusive_scan(s->hist, t->nkeys + 1, s->scan_tmp, st));
+    FG_CUDA(cudaMemcpyAsync(s->cursor, s->hist, sizeof(uint32_t) * (t->nkeys + 1), cudaMemcpyDeviceToDevice, st));
     if (ev) FG_CUDA(cudaEventRecord(ev[1], st));
     if (Np > 0) {
         if (pos_prec == 4)
             paint_scatter_kernel<float><<<gp, 256, 0, st>>>((const float *)x, (const float *)y, (const float *)z,
-                                                           Np, pp, s->key, s->rank, s->hist, (uint4 *)s->sorted,
-                                                           ds);
+                                                           Np, pp, s->cursor, (uint4 *)s->sorted, ds);
         else
             paint_scatter_kernel<double><<<gp, 256, 0, st>>>((const double *)x, (const double *)y,
-                                                            (const double *)z, Np, pp, s->key, s->rank, s->hist,
+                                                            (const double *)z, Np, pp, s->cursor,
                                                             (Rec<double>::type *)s->sorted, nullptr);
         FG_LAUNCHED(1);
     }

@@ -57,8 +57,9 @@ void *fftgal_device_grid(fft_t *grid);
 /* copy Ng3_pad values of the grid's precision between the canonical grid and
  * a caller buffer (host or device, any CUDA-visible pointer):
  * to_grid = 1 copies buf -> grid, 0 copies grid -> buf.  The copy waits for
- * the grid's stream and runs on the legacy default stream; work that fills
- * `buf` on other non-blocking streams must be complete first. */
+ * the grid's stream, runs on the legacy default stream and is complete when
+ * the call returns; work that fills `buf` on other non-blocking streams must
+ * be complete first. */
 int fftgal_copy_grid(fft_t *grid, void *buf, int to_grid);
 /* wait for all queued work of the grid */
 int fftgal_synchronize(fft_t *grid);
@@ -191,15 +192,6 @@ double fftgal_alias_envelope(double u);
 int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms[3]);
 /* measure now (clears the grid) and keep the fastest shapes on this grid */
 int fftgal_plan_autotune(fft_t *grid, double ms[3]);
-/* Forward FP32 transforms run their first two passes (r2c along k, then j)
- * slab by slab: `planes` i planes of both interlacing grids per slab (a single
- * grid takes twice as many), so that the j pass reads the k pass's output from
- * L2 instead of HBM.  The default fills about half the L2 cache (8 planes at
- * Ng = 1024 on GB300; 0 when a whole grid fits).  planes >= 0 sets it (0: no
- * slabs, the k pass over the whole grid, then the j pass), -1 only queries;
- * returns the value in use.  Results are bit-identical for every value (the
- * same kernels transform the same rows and columns). */
-int fftgal_fft_slab_planes(fft_t *grid, int planes);
 /* in-place unnormalised FFTs of length N (a power of two from 4 to 2048) along
  * strided columns of complex FP32 data in GPU memory, with the kernels of the
  * grid's j and i passes: element n of column c (c < ncols) of batch b

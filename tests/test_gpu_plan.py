@@ -113,27 +113,44 @@ def test_unwritable_plan_file_is_not_fatal(fg, tmp_path):
     assert not path.exists()
 
 
-@pytest.mark.parametrize("Ng", [64, 256])
-def test_kj_slabs_bit_identical(fg, Ng):
-    """The forward k + j passes run slab by slab of i planes (the j pass reads
-    the k pass's output from L2): every slab size, including one that leaves
-    a shorter last slab, gives the k-space grid of the unslabbed passes bit
-    for bit, for the interlaced pair (fft_p2k) and a single grid (fft_x2k)."""
-    rng = np.random.default_rng(5)
-    x, y, z = (rng.uniform(0, L_BOX, 100_000) for _ in range(3))
-    g = fg.Grid(Ng, L_BOX, precision="f32", host_view="sync")
-    cat = fg.Catalog(x, y, z, V=L_BOX ** 3)
-    assert g.slab_planes() >= 0
-    want_p2k = want_x2k = None
-    for planes in (0, 1, 7, Ng // 2):
-        assert g.slab_planes(planes) == planes
-        g.p2k(cat)
-        got_p2k = g.f.copy()
-        g.p2g(cat, [0.0, 0.0, 0.0])
-        g.x2k(0)
-        got_x2k = g.f.copy()
-        if want_p2k is None:
-            want_p2k, want_x2k = got_p2k, got_x2k
-        else:
-            assert got_p2k.tobytes() == want_p2k.tobytes(), planes
-            assert got_x2k.tobytes() == want_x2k.tobytes(), planes
+_TMA_CHILD = r"""
+import sys, torch
+sys.path.insert(0, sys.argv[1])
+import fftgal_gb300 as fg
+Ng = int(sys.argv[2])
+Ngp = 2 * (Ng // 2 + 1)
+g = fg.Grid(Ng, float(Ng), precision="f32", host_view="lazy")
+gen = torch.Generator(device="cuda").manual_seed(Ng)
+x = torch.randn((Ng, Ng, Ngp), generator=gen, device="cuda", dtype=torch.float32)
+w = (torch.arange(x.numel(), device="cuda", dtype=torch.int64) % 1000003) + 1
+def digest(t):
+    b = t.view(torch.int32).reshape(-1).to(torch.int64)
+    return [int(b.sum()), int((b * w).sum()), int((b ^ (w * 2654435761)).sum())]
+g.copy_from(x.data_ptr())
+g.x2k(0)
+g.copy_to(x.data_ptr())
+k = digest(x)
+g.k2x(0)
+g.copy_to(x.data_ptr())
+print(k + digest(x))
+"""
+
+
+@pytest.mark.parametrize("Ng", [512, 1024])
+def test_tma_i_pass_bit_identical(fg, tmp_path, Ng):
+    """The TMA-staged i pass (Ng = 512 and 1024) transforms every column with
+    the same decomposition and twiddles as the register-staged column kernel:
+    forward and backward grids are bit-identical to a run with FFTGAL_TMA=0
+    (compared through integer checksums of their bits)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = {}
+    for tma in ("1", "0"):
+        env = dict(os.environ, FFTGAL_TMA=tma, FFTGAL_QUIET="1")
+        r = subprocess.run([sys.executable, "-c", _TMA_CHILD, root, str(Ng)], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs[tma] = r.stdout.strip().splitlines()[-1]
+    assert outs["1"] == outs["0"]
