@@ -78,28 +78,23 @@ __device__ __forceinline__ float2 twid(const float2 *__restrict__ W, int t, int 
 
 // ---- strided axis: C columns per CTA, threads = C * N2 ---------------------------
 // element n of column c of batch b: base + b*bs + n*es + c0 + c (complex units)
-template <int N1, int N2>
-__global__ void __launch_bounds__(512)
-fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC,
-                 const float2 *__restrict__ W, int sign) {
-    constexpr int N = N1 * N2;
-    extern __shared__ __align__(16) float2 S[];
+// One tile: columns c0 .. c0 + C - 1 at `base` (= g + b*bs + c0), `left`
+// columns of them valid; threads t < nthr of the CTA (nthr >= C*N2).  CG:
+// loads bypass L1 (data written by other CTAs of the cluster).
+template <int N1, int N2, bool CG>
+__device__ __forceinline__ void cols_tile(float2 *base, int left, long es, int logC, const float2 *__restrict__ W,
+                                          int sign, float2 *S, int t, int nthr) {
     const int C = 1 << logC;
     const int P = N1 * C + 8;  // shared pitch per n2
-    const int ncb = (ncols + C - 1) >> logC;
-    const int cb = blockIdx.x % ncb;
-    const long batch = blockIdx.x / ncb;
-    float2 *g = blockIdx.y == 0 ? g0 : g1;
-    const int c0 = cb << logC;
-    float2 *base = g + batch * bs + c0;
-    const int t = threadIdx.x;
-    {
+    if (t < C * N2) {
         const int c = t & (C - 1), n2 = t >> logC;
-        const bool ok = c0 + c < ncols;
+        const bool ok = c < left;
         float2 v[N1];
 #pragma unroll
-        for (int n1 = 0; n1 < N1; ++n1)
-            v[n1] = ok ? base[(long)(N2 * n1 + n2) * es + c] : make_float2(0.f, 0.f);
+        for (int n1 = 0; n1 < N1; ++n1) {
+            const float2 *src = &base[(long)(N2 * n1 + n2) * es + c];
+            v[n1] = ok ? (CG ? __ldcg(src) : *src) : make_float2(0.f, 0.f);
+        }
         reg_fft<N1>(v, sign);
         if constexpr (N2 > 1) {
 #pragma unroll
@@ -115,18 +110,31 @@ fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC,
     }
     if constexpr (N2 > 1) {
         __syncthreads();
-        for (int s = t; s < C * N1; s += blockDim.x) {
+        for (int s = t; s < C * N1; s += nthr) {
             const int c = s & (C - 1), k1 = s >> logC;
             float2 u[N2];
 #pragma unroll
             for (int n2 = 0; n2 < N2; ++n2) u[n2] = S[n2 * P + k1 * C + c];
             reg_fft<N2>(u, sign);
-            if (c0 + c < ncols)
+            if (c < left)
 #pragma unroll
                 for (int k2 = 0; k2 < N2; ++k2) base[(long)(k1 + N1 * k2) * es + c] = u[k2];
         }
     }
-    (void)N;
+}
+
+template <int N1, int N2>
+__global__ void __launch_bounds__(512)
+fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC,
+                 const float2 *__restrict__ W, int sign) {
+    extern __shared__ __align__(16) float2 S[];
+    const int C = 1 << logC;
+    const int ncb = (ncols + C - 1) >> logC;
+    const int cb = blockIdx.x % ncb;
+    const long batch = blockIdx.x / ncb;
+    float2 *g = blockIdx.y == 0 ? g0 : g1;
+    const int c0 = cb << logC;
+    cols_tile<N1, N2, false>(g + batch * bs + c0, ncols - c0, es, logC, W, sign, S, threadIdx.x, blockDim.x);
 }
 
 // ---- strided axis of length 2048 = 32 x 64 ---------------------------------------------
@@ -191,16 +199,13 @@ fft2_cols2048_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int lo
 // ---- k axis, forward r2c: R rows per CTA, threads = R * N2 ---------------------------
 // Each real row of Ng = 2M values is read as M packed complex values
 // z[m] = x[2m] + i x[2m+1]; X[k] = E[k] + W_Ng^k O[k] for k = 0..M.
+// One tile: rows row0 .. row0 + R - 1 (of nrows) of g; threads t < nthr.
 template <int N1, int N2>
-__global__ void __launch_bounds__(512)
-fft2_k_r2c_kernel(float *g0, float *g1, long nrows, int Ng_pad, int R,
-                  const float2 *__restrict__ W, const float2 *__restrict__ rtw) {
+__device__ __forceinline__ void kr2c_tile(float *g, long nrows, int Ng_pad, int R, long row0,
+                                          const float2 *__restrict__ W, const float2 *__restrict__ rtw, float2 *S,
+                                          int t, int nthr) {
     constexpr int M = N1 * N2;
     constexpr int P = N2 * (N1 + 1);  // shared row pitch (step-1 layout, padded)
-    extern __shared__ __align__(16) float2 S[];
-    float *g = blockIdx.y == 0 ? g0 : g1;
-    const long row0 = (long)blockIdx.x * R;
-    const int t = threadIdx.x;
     {
         const int n2 = t % N2, r = t / N2;
         const bool ok = r < R && row0 + r < nrows;
@@ -220,7 +225,6 @@ fft2_k_r2c_kernel(float *g0, float *g1, long nrows, int Ng_pad, int R,
     // step 2: results in registers until every thread has read its inputs
     constexpr int ROUNDS_MAX = N1 / N2 > 0 ? N1 / N2 : 1;
     float2 res[ROUNDS_MAX][N2];
-    const int nthr = blockDim.x;
 #pragma unroll
     for (int q = 0; q < ROUNDS_MAX; ++q) {
         const int s = t + q * nthr;
@@ -254,6 +258,63 @@ fft2_k_r2c_kernel(float *g0, float *g1, long nrows, int Ng_pad, int R,
         const float2 D = csub(z1, z2);
         const float2 O = make_float2(0.5f * D.y, -0.5f * D.x);
         reinterpret_cast<float2 *>(g + (row0 + r) * Ng_pad)[k] = cadd(E, cmul(__ldg(&rtw[k]), O));
+    }
+}
+
+template <int N1, int N2>
+__global__ void __launch_bounds__(512)
+fft2_k_r2c_kernel(float *g0, float *g1, long nrows, int Ng_pad, int R,
+                  const float2 *__restrict__ W, const float2 *__restrict__ rtw) {
+    extern __shared__ __align__(16) float2 S[];
+    kr2c_tile<N1, N2>(blockIdx.y == 0 ? g0 : g1, nrows, Ng_pad, R, (long)blockIdx.x * R, W, rtw, S, threadIdx.x,
+                      blockDim.x);
+}
+
+// ---- k and j passes of one i plane per thread-block cluster ----------------------------
+// Ng = 512 or 1024.  A cluster of CS CTAs (one per SM) takes one i plane of
+// one grid at a time: every CTA transforms Ng / CS of its rows along k (r2c,
+// kr2c_tile, 32 rows per step), the cluster barrier (release / acquire)
+// publishes them, then every CTA transforms its share of the plane's columns
+// along j (cols_tile, 512 / N2 columns per step, loads from L2).  A plane is
+// 2 MB (Ng = 512) or 4.2 MB: with CS = 8 the planes in flight (one per
+// cluster) fill well under the L2, so the j step reads the k step's output
+// from L2, and each plane crosses HBM once in each direction instead of twice.
+// The column Ng / 2 is transformed by the cluster's CTA 0 after its share.
+template <int KN1, int KN2, int CN1, int CN2>
+__global__ void __launch_bounds__(512, 1)
+fft2_kj_cluster_kernel(float *g0, float *g1, int ngrids, int Ng, const float2 *__restrict__ Wk,
+                       const float2 *__restrict__ rtw, const float2 *__restrict__ Wj) {
+    extern __shared__ __align__(16) float2 S[];
+    static_assert(KN1 * KN2 * 2 == CN1 * CN2, "k and j lengths");
+    constexpr int N = CN1 * CN2, R = 512 / KN2, logC = CN2 == 32 ? 4 : 5, C = 1 << logC;
+    static_assert(C * CN2 == 512, "one column tile per 512 threads");
+    unsigned rank, cid, ncl, cs;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(cid));
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(ncl));
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(cs));
+    const int nh = N / 2 + 1, Ng_pad = 2 * nh;
+    const int t = threadIdx.x;
+    const int rows_per = N / (int)cs;
+    const int ngroups = (N / 2) / C;  // full column tiles; column N/2 separately
+    for (long job = cid; job < (long)ngrids * N; job += ncl) {
+        const int g = (int)(job / N), i = (int)(job % N);
+        float *plane = (g ? g1 : g0) + (long)i * N * Ng_pad;
+        for (int r0 = (int)rank * rows_per; r0 < ((int)rank + 1) * rows_per; r0 += R) {
+            kr2c_tile<KN1, KN2>(plane, N, Ng_pad, R, r0, Wk, rtw, S, t, 512);
+            __syncthreads();
+        }
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+        float2 *pc = reinterpret_cast<float2 *>(plane);
+        for (int q = (int)rank; q < ngroups; q += (int)cs) {
+            cols_tile<CN1, CN2, true>(pc + q * C, C, nh, logC, Wj, -1, S, t, 512);
+            __syncthreads();
+        }
+        if (rank == 0) {
+            cols_tile<CN1, CN2, true>(pc + N / 2, 1, nh, logC, Wj, -1, S, t, 512);
+            __syncthreads();
+        }
     }
 }
 
@@ -542,6 +603,57 @@ int fft2_default_shape(int Ng, int which) {
 
 int fft2_prepare() { return ensure_w32(); }
 
+// ---- k and j passes per cluster ------------------------------------------------------------
+bool fft2_kj_cluster_supported(int Ng, int prec) {
+    static const int off = [] {
+        const char *e = getenv("FFTGAL_KJ_CLUSTER");
+        return e && e[0] == '0';
+    }();
+    return !off && prec == 4 && (Ng == 512 || Ng == 1024);
+}
+
+template <typename K>
+static int launch_kj_cluster(K kernel, size_t smem, int Ng, const void *Wk, const void *rtw, const void *Wj, void *g0,
+                             void *g1, int ngrids, cudaStream_t s) {
+    constexpr int kCS = 8;  // CTAs per cluster (portable size)
+    FG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kCS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(512, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(kCS, 1, 1);
+    int ncl = 0;
+    FG_CUDA(cudaOccupancyMaxActiveClusters(&ncl, kernel, &cfg));
+    if (ncl < 1) return set_error(ERR_UNSUPPORTED, "k+j cluster pass: no cluster of %d CTAs fits an SM group", kCS);
+    const long jobs = (long)ngrids * Ng;
+    if (ncl > jobs) ncl = (int)jobs;
+    cfg.gridDim = dim3((unsigned)(ncl * kCS), 1, 1);
+    FG_CUDA(cudaLaunchKernelEx(&cfg, kernel, (float *)g0, (float *)g1, ngrids, Ng, (const float2 *)Wk,
+                               (const float2 *)rtw, (const float2 *)Wj));
+    FG_LAUNCHED(1);
+    return OK;
+}
+
+int fft2_kj_cluster(int Ng, const void *Wk, const void *rtw, const void *Wj, void *g0, void *g1, int ngrids,
+                    cudaStream_t s) {
+    FG_TRY(ensure_w32());
+    if (!fft2_kj_cluster_supported(Ng, 4)) return set_error(ERR_UNSUPPORTED, "k+j cluster pass: Ng=%d", Ng);
+    void *b = ngrids > 1 ? g1 : g0;
+    if (Ng == 1024) {
+        const size_t smem = k_smem(32, 16, 32) > cols_smem(32, 32, 4) ? k_smem(32, 16, 32) : cols_smem(32, 32, 4);
+        return launch_kj_cluster(fft2_kj_cluster_kernel<32, 16, 32, 32>, smem, Ng, Wk, rtw, Wj, g0, b, ngrids, s);
+    }
+    const size_t smem = k_smem(16, 16, 32) > cols_smem(32, 16, 5) ? k_smem(16, 16, 32) : cols_smem(32, 16, 5);
+    return launch_kj_cluster(fft2_kj_cluster_kernel<16, 16, 32, 16>, smem, Ng, Wk, rtw, Wj, g0, b, ngrids, s);
+}
+
 // ---- TMA-staged i pass ------------------------------------------------------------------
 using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -582,11 +694,14 @@ static int plane_tensor_map(CUtensorMap *tm, void *grid, int Ng) {
 }
 
 bool fft2_tma_supported(int Ng, int prec) {
-    static const int off = [] {
+    // off by default: with 64-byte rows at the plane stride the TMA pass
+    // measured 7.8 ms against 4.7 ms for fft2_cols_kernel (16 columns, 128-byte
+    // rows) at Ng = 1024; FFTGAL_TMA=1 selects it
+    static const int on = [] {
         const char *e = getenv("FFTGAL_TMA");
-        return e && e[0] == '0';
+        return e && e[0] == '1';
     }();
-    return !off && prec == 4 && (Ng == 512 || Ng == 1024);
+    return on && prec == 4 && (Ng == 512 || Ng == 1024);
 }
 
 int fft2_cols_tma(int Ng, const void *W, void *g0, void *g1, int ngrids, int sign, cudaStream_t s) {
