@@ -1057,16 +1057,9 @@ static int power_f32_run(fft_t *grid, const float *x, const float *y, const floa
     FG_TRY(paint(&g->tiling, &g->scratch, 4, px, py, pz, 4, Np, Hinv, spec, ngr, st, tm ? ev + 2 : nullptr,
                  vel ? &rsd : nullptr));
     void *grids[2] = {g->d_f, g->d_aux};
-    // k and j passes (one cluster kernel where supported: the fft_k stage then
-    // times both and fft_j is empty)
-    if (fft2_kj_cluster_supported(grid->Ng, g->prec)) {
-        FG_TRY(fft_pass_kj(&g->fft, grids, ngr, st));
-        if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
-    } else {
-        FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
-        if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
-        FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
-    }
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, ngr, st));
+    if (tm) FG_CUDA(cudaEventRecord(ev[6], st));
+    FG_TRY(fft_pass_j(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[7], st));
     FG_TRY(fft_pass_i(&g->fft, grids, ngr, -1, st));
     if (tm) FG_CUDA(cudaEventRecord(ev[8], st));
@@ -1224,7 +1217,8 @@ static int enqueue_catalog(fft_t *grid, int b, long capNp, BinGeometry *geo, cud
     FG_TRY(paint(&g->tiling, &g->scratch, 4, d, d + capNp, d + 2 * capNp, 4, capNp, Ng / grid->L, spec, 2, st,
                  nullptr, nullptr, g->d_scal + b));
     void *grids[2] = {g->d_f, g->d_aux};
-    FG_TRY(fft_pass_kj(&g->fft, grids, 2, st));
+    FG_TRY(fft_pass_k_r2c(&g->fft, grids, 2, st));
+    FG_TRY(fft_pass_j(&g->fft, grids, 2, -1, st));
     FG_TRY(fft_pass_i(&g->fft, grids, 2, -1, st));
     BinFinish fin;
     fin.A = g->d_f;

@@ -573,16 +573,9 @@ int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaS
     return cols_pass(p, grids, ngrids, sign, (long)p->Ng * p->nh, p->nh, s, p->tune[2]);
 }
 
-int fft_pass_kj(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s) {
-    if (fft2_kj_cluster_supported(p->Ng, p->prec))
-        return fft2_kj_cluster(p->Ng, p->half.tw, p->rtw, p->axis.tw, grids[0], ngrids > 1 ? grids[1] : grids[0],
-                               ngrids, s);
-    FG_TRY(fft_pass_k_r2c(p, grids, ngrids, s));
-    return fft_pass_j(p, grids, ngrids, -1, s);
-}
-
 int fft_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s) {
-    FG_TRY(fft_pass_kj(p, grids, ngrids, s));
+    FG_TRY(fft_pass_k_r2c(p, grids, ngrids, s));
+    FG_TRY(fft_pass_j(p, grids, ngrids, -1, s));
     FG_TRY(fft_pass_i(p, grids, ngrids, -1, s));
     return OK;
 }

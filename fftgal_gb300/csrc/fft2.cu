@@ -79,9 +79,8 @@ __device__ __forceinline__ float2 twid(const float2 *__restrict__ W, int t, int 
 // ---- strided axis: C columns per CTA, threads = C * N2 ---------------------------
 // element n of column c of batch b: base + b*bs + n*es + c0 + c (complex units)
 // One tile: columns c0 .. c0 + C - 1 at `base` (= g + b*bs + c0), `left`
-// columns of them valid; threads t < nthr of the CTA (nthr >= C*N2).  CG:
-// loads bypass L1 (data written by other CTAs of the cluster).
-template <int N1, int N2, bool CG>
+// columns of them valid; threads t < nthr of the CTA (nthr >= C*N2).
+template <int N1, int N2>
 __device__ __forceinline__ void cols_tile(float2 *base, int left, long es, int logC, const float2 *__restrict__ W,
                                           int sign, float2 *S, int t, int nthr) {
     const int C = 1 << logC;
@@ -93,7 +92,7 @@ __device__ __forceinline__ void cols_tile(float2 *base, int left, long es, int l
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) {
             const float2 *src = &base[(long)(N2 * n1 + n2) * es + c];
-            v[n1] = ok ? (CG ? __ldcg(src) : *src) : make_float2(0.f, 0.f);
+            v[n1] = ok ? *src : make_float2(0.f, 0.f);
         }
         reg_fft<N1>(v, sign);
         if constexpr (N2 > 1) {
@@ -134,7 +133,7 @@ fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC,
     const long batch = blockIdx.x / ncb;
     float2 *g = blockIdx.y == 0 ? g0 : g1;
     const int c0 = cb << logC;
-    cols_tile<N1, N2, false>(g + batch * bs + c0, ncols - c0, es, logC, W, sign, S, threadIdx.x, blockDim.x);
+    cols_tile<N1, N2>(g + batch * bs + c0, ncols - c0, es, logC, W, sign, S, threadIdx.x, blockDim.x);
 }
 
 // ---- strided axis of length 2048 = 32 x 64 ---------------------------------------------
@@ -268,54 +267,6 @@ fft2_k_r2c_kernel(float *g0, float *g1, long nrows, int Ng_pad, int R,
     extern __shared__ __align__(16) float2 S[];
     kr2c_tile<N1, N2>(blockIdx.y == 0 ? g0 : g1, nrows, Ng_pad, R, (long)blockIdx.x * R, W, rtw, S, threadIdx.x,
                       blockDim.x);
-}
-
-// ---- k and j passes of one i plane per thread-block cluster ----------------------------
-// Ng = 512 or 1024.  A cluster of CS CTAs (one per SM) takes one i plane of
-// one grid at a time: every CTA transforms Ng / CS of its rows along k (r2c,
-// kr2c_tile, 32 rows per step), the cluster barrier (release / acquire)
-// publishes them, then every CTA transforms its share of the plane's columns
-// along j (cols_tile, 512 / N2 columns per step, loads from L2).  A plane is
-// 2 MB (Ng = 512) or 4.2 MB: with CS = 8 the planes in flight (one per
-// cluster) fill well under the L2, so the j step reads the k step's output
-// from L2, and each plane crosses HBM once in each direction instead of twice.
-// The column Ng / 2 is transformed by the cluster's CTA 0 after its share.
-template <int KN1, int KN2, int CN1, int CN2>
-__global__ void __launch_bounds__(512, 1)
-fft2_kj_cluster_kernel(float *g0, float *g1, int ngrids, int Ng, const float2 *__restrict__ Wk,
-                       const float2 *__restrict__ rtw, const float2 *__restrict__ Wj) {
-    extern __shared__ __align__(16) float2 S[];
-    static_assert(KN1 * KN2 * 2 == CN1 * CN2, "k and j lengths");
-    constexpr int N = CN1 * CN2, R = 512 / KN2, logC = CN2 == 32 ? 4 : 5, C = 1 << logC;
-    static_assert(C * CN2 == 512, "one column tile per 512 threads");
-    unsigned rank, cid, ncl, cs;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
-    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(cid));
-    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(ncl));
-    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(cs));
-    const int nh = N / 2 + 1, Ng_pad = 2 * nh;
-    const int t = threadIdx.x;
-    const int rows_per = N / (int)cs;
-    const int ngroups = (N / 2) / C;  // full column tiles; column N/2 separately
-    for (long job = cid; job < (long)ngrids * N; job += ncl) {
-        const int g = (int)(job / N), i = (int)(job % N);
-        float *plane = (g ? g1 : g0) + (long)i * N * Ng_pad;
-        for (int r0 = (int)rank * rows_per; r0 < ((int)rank + 1) * rows_per; r0 += R) {
-            kr2c_tile<KN1, KN2>(plane, N, Ng_pad, R, r0, Wk, rtw, S, t, 512);
-            __syncthreads();
-        }
-        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-        float2 *pc = reinterpret_cast<float2 *>(plane);
-        for (int q = (int)rank; q < ngroups; q += (int)cs) {
-            cols_tile<CN1, CN2, true>(pc + q * C, C, nh, logC, Wj, -1, S, t, 512);
-            __syncthreads();
-        }
-        if (rank == 0) {
-            cols_tile<CN1, CN2, true>(pc + N / 2, 1, nh, logC, Wj, -1, S, t, 512);
-            __syncthreads();
-        }
-    }
 }
 
 // ---- widely strided axis (the i pass), columns staged by TMA ----------------------------------
@@ -602,57 +553,6 @@ int fft2_default_shape(int Ng, int which) {
 }
 
 int fft2_prepare() { return ensure_w32(); }
-
-// ---- k and j passes per cluster ------------------------------------------------------------
-bool fft2_kj_cluster_supported(int Ng, int prec) {
-    static const int off = [] {
-        const char *e = getenv("FFTGAL_KJ_CLUSTER");
-        return e && e[0] == '0';
-    }();
-    return !off && prec == 4 && (Ng == 512 || Ng == 1024);
-}
-
-template <typename K>
-static int launch_kj_cluster(K kernel, size_t smem, int Ng, const void *Wk, const void *rtw, const void *Wj, void *g0,
-                             void *g1, int ngrids, cudaStream_t s) {
-    constexpr int kCS = 8;  // CTAs per cluster (portable size)
-    FG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kCS;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(512, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cfg.gridDim = dim3(kCS, 1, 1);
-    int ncl = 0;
-    FG_CUDA(cudaOccupancyMaxActiveClusters(&ncl, kernel, &cfg));
-    if (ncl < 1) return set_error(ERR_UNSUPPORTED, "k+j cluster pass: no cluster of %d CTAs fits an SM group", kCS);
-    const long jobs = (long)ngrids * Ng;
-    if (ncl > jobs) ncl = (int)jobs;
-    cfg.gridDim = dim3((unsigned)(ncl * kCS), 1, 1);
-    FG_CUDA(cudaLaunchKernelEx(&cfg, kernel, (float *)g0, (float *)g1, ngrids, Ng, (const float2 *)Wk,
-                               (const float2 *)rtw, (const float2 *)Wj));
-    FG_LAUNCHED(1);
-    return OK;
-}
-
-int fft2_kj_cluster(int Ng, const void *Wk, const void *rtw, const void *Wj, void *g0, void *g1, int ngrids,
-                    cudaStream_t s) {
-    FG_TRY(ensure_w32());
-    if (!fft2_kj_cluster_supported(Ng, 4)) return set_error(ERR_UNSUPPORTED, "k+j cluster pass: Ng=%d", Ng);
-    void *b = ngrids > 1 ? g1 : g0;
-    if (Ng == 1024) {
-        const size_t smem = k_smem(32, 16, 32) > cols_smem(32, 32, 4) ? k_smem(32, 16, 32) : cols_smem(32, 32, 4);
-        return launch_kj_cluster(fft2_kj_cluster_kernel<32, 16, 32, 32>, smem, Ng, Wk, rtw, Wj, g0, b, ngrids, s);
-    }
-    const size_t smem = k_smem(16, 16, 32) > cols_smem(32, 16, 5) ? k_smem(16, 16, 32) : cols_smem(32, 16, 5);
-    return launch_kj_cluster(fft2_kj_cluster_kernel<16, 16, 32, 16>, smem, Ng, Wk, rtw, Wj, g0, b, ngrids, s);
-}
 
 // ---- TMA-staged i pass ------------------------------------------------------------------
 using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,

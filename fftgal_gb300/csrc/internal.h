@@ -85,8 +85,7 @@ int fft_c2r(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_k_r2c(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
 int fft_pass_j(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
 int fft_pass_i(const FftPlan *p, void *const *grids, int ngrids, int sign, cudaStream_t s);
-// the forward k and j passes: one cluster kernel where supported, else the two passes
-int fft_pass_kj(const FftPlan *p, void *const *grids, int ngrids, cudaStream_t s);
+
 // two-level FP32 kernels (fft2.cu) for power-of-two Ng in [4, 1024]
 bool fft2_supported(int Ng, int prec);
 int fft2_cols(int N, const void *W, void *g0, void *g1, int ngrids, int ncols, long es, long bs,
@@ -99,12 +98,6 @@ bool fft2_valid_shape(int Ng, int which, int v);
 int fft2_default_shape(int Ng, int which);
 // device twiddle tables of the two-level kernels (built once per device)
 int fft2_prepare();
-// forward k (r2c) and j passes of FP32 grids (Ng = 512 or 1024;
-// FFTGAL_KJ_CLUSTER=0 turns it off) with one thread-block cluster per i plane:
-// the j step reads the k step's output from L2
-bool fft2_kj_cluster_supported(int Ng, int prec);
-int fft2_kj_cluster(int Ng, const void *Wk, const void *rtw, const void *Wj, void *g0, void *g1, int ngrids,
-                    cudaStream_t s);
 // TMA-staged strided pass along i of FP32 grids (Ng = 512 or 1024; selected by
 // FFTGAL_TMA=1): the i pass of fft_pass_i; fft2_tma_check reports (and
 // clears) a time-out of its bounded mbarrier waits -- call it after a sync

@@ -138,18 +138,18 @@ print(k + digest(x))
 
 @pytest.mark.parametrize("Ng", [512, 1024])
 def test_tma_i_pass_bit_identical(fg, tmp_path, Ng):
-    """The TMA-staged i pass and the per-cluster k + j passes (Ng = 512 and
-    1024) transform every row and column with the same decompositions and
-    twiddles as the separate register-staged kernels: forward and backward
-    grids are bit-identical to a run with FFTGAL_TMA=0 and FFTGAL_KJ_CLUSTER=0
-    (compared through integer checksums of their bits)."""
+    """The TMA-staged i pass (Ng = 512 and 1024, selected by FFTGAL_TMA=1)
+    transforms every column with the same decomposition and twiddles as the
+    register-staged column kernel: forward and backward grids are
+    bit-identical to a run without it (compared through integer checksums of
+    their bits)."""
     import os
     import subprocess
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     outs = {}
-    for tma in ("1", "0"):  # both special paths on, then both off
-        env = dict(os.environ, FFTGAL_TMA=tma, FFTGAL_KJ_CLUSTER=tma, FFTGAL_QUIET="1")
+    for tma in ("1", "0"):
+        env = dict(os.environ, FFTGAL_TMA=tma, FFTGAL_QUIET="1")
         r = subprocess.run([sys.executable, "-c", _TMA_CHILD, root, str(Ng)], env=env,
                            capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
