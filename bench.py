@@ -62,6 +62,10 @@ def parse(argv=None):
                     help="plan file of the FFT autotuner (default: one in the temporary directory)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="run only warmup+this many steps, no e2e/cpu legs (for ncu)")
+    ap.add_argument("--workload", default="headline", choices=["headline", "mixed64"],
+                    help="mixed64: 64 lognormal redshift-space mocks with Np log-uniform in [2e6, 2e7], "
+                         "Ng from {256, 384, 512} and fold factors from {1, 2, 4}, through one "
+                         "fftgal_power_mixed_f32 call per step")
     ap.add_argument("--launch-check", action="store_true",
                     help="exercise the N-rank launch and the max-over-ranks reduction without a GPU "
                          "(gloo) and print the JSON line")
@@ -337,6 +341,76 @@ def parity_block(res, Ng: int, Np: int, mock: str, live):
     return out
 
 
+def run_mixed(args):
+    """--workload mixed64: the covariance-set configuration.  64 lognormal mocks
+    (512^3 Gaussian field, P(k) = 1e4 (k/0.1)^-1.5 exp(-(k/0.5)^2), Poisson
+    sampled, displaced by the Zel'dovich displacement and shifted along z by
+    f Psi_z with f = 0.8, independent seeds) generated on the GPU and kept
+    there; one step = one fftgal_power_mixed_f32 call over all 64."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    import fftgal_gb300 as fg
+    from fftgal_gb300 import mocks
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(64)
+    ncat, f = 64, 0.8
+    Nps = 10 ** rng.uniform(np.log10(2e6), np.log10(2e7), ncat)
+    Ngs = rng.choice([256, 384, 512], ncat)
+    folds = rng.choice([1, 2, 4], ncat)
+    cats = []
+    for c in range(ncat):
+        x, y, z, vx, vy, vz = mocks.lognormal_catalog(512, L_BOX, float(Nps[c]), seed=1000 + c, f=f, device=dev)
+        cats.append(torch.stack([x + vx / f, y + vy / f, z + vz / f + vz]).contiguous())
+        del x, y, z, vx, vy, vz
+    torch.cuda.empty_cache()
+    n_part = sum(int(t.shape[1]) for t in cats)
+    lib = fg.lib()
+    ptr = [(C.c_void_p * ncat)(*[t[a].data_ptr() for t in cats]) for a in range(3)]
+    Np = np.array([t.shape[1] for t in cats], dtype=np.int64)
+    V = np.full(ncat, L_BOX ** 3)
+    L = np.ascontiguousarray(L_BOX / folds, dtype=np.float64)
+    dK = np.ascontiguousarray(2 * np.pi / L, dtype=np.float64)
+    Ngc = np.ascontiguousarray(Ngs, dtype=np.int32)
+    los = np.array(LOS)
+    tabs = []
+    for c in range(ncat):
+        NK = fg.nk(int(Ngc[c]), float(L[c]), float(dK[c]))
+        tabs.append([np.zeros(NK), np.zeros(NK, dtype=np.int64), np.zeros(NK * 4), np.zeros(NK * NMU),
+                     np.zeros(NK * NMU, dtype=np.int64), np.zeros(NK * NMU)])
+    outs = [(C.c_void_p * ncat)(*[tabs[c][q].ctypes.data for c in range(ncat)]) for q in range(6)]
+    dp = C.POINTER(C.c_double)
+
+    def step():
+        rc = lib.fftgal_power_mixed_f32(ncat, ptr[0], ptr[1], ptr[2], Np.ctypes.data_as(C.POINTER(C.c_long)),
+                                        V.ctypes.data_as(dp), Ngc.ctypes.data_as(C.POINTER(C.c_int)),
+                                        L.ctypes.data_as(dp), los.ctypes.data_as(dp), dK.ctypes.data_as(dp), NMU,
+                                        *outs)
+        if rc != 0:
+            raise RuntimeError(lib.fftgal_last_error().decode())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()  # returns after the last catalog's tables are on the host
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    groups = sorted({(int(a), int(b)) for a, b in zip(Ngs, folds)})
+    print(json.dumps({
+        "metric": "catalogs/s, 64 mixed lognormal RSD mocks (Ng 256/384/512, folds 1/2/4, Np 2e6-2e7)",
+        "value": ncat * args.steps / wall, "unit": "catalogs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (lognormal mocks generated on the GPU, seeds 1000-1063)",
+        "config": {"workload": "mixed64", "catalogs": ncat, "particles": n_part, "groups_Ng_fold": groups,
+                   "Nmu": NMU, "positions": "device-resident", "timing": "host wall clock around the calls"},
+    }), flush=True)
+
+
 def learned_leg(args, fg, grid, stream, barrier, ptrs, Np, dK, ms_interlaced, res_interlaced):
     """Learned aliasing correction on the same catalog: one paint + FFT, the
     multipoles corrected by the committed perceptron (fftgal_power_learned_f32),
@@ -602,6 +676,8 @@ def main(argv=None):
         launch_check(args)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.workload == "mixed64":
+        run_mixed(args)
     else:
         run_ours(args)
 

@@ -96,6 +96,10 @@ SIGNATURES = {
     "fftgal_window_box": (C.c_int, [_P_F, C.c_int]),
     "fftgal_window_sphere": (C.c_int, [_P_F, C.c_int]),
     "fftgal_dl_sub": (C.c_int, [_P_F, C.c_int, C.c_int, C.c_int, _dp, C.c_double, _dp]),
+    "fftgal_power_mixed_f32": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp,
+                                          C.POINTER(C.c_int), _dp, _dp, _dp, C.c_int, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fftgal_power_mixed_release": (C.c_int, []),
     "fftgal_power_batch_f32": (C.c_int, [_P_F, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _lp, _dp, _dp,
                                          C.c_double, C.c_int, _dp, _lp, _dp, _dp, _lp, _dp]),
     "fftgal_mlp_nparams": (C.c_int, []),
@@ -534,6 +538,37 @@ def power_bins_noalloc(fk: int, Ng: int, L: float, V: float, Np: int, los, dK: f
                                            P.ctypes.data_as(_dp), Km.ctypes.data_as(_dp), Nm.ctypes.data_as(_lp),
                                            Pm.ctypes.data_as(_dp), stream))
     return dict(K=K, N=N, P=P, Kmu=Km, Nmu=Nm, Pmu=Pm)
+
+
+def power_mixed_f32(cats, V, Ng, L, los, dK, Nmu: int = 3) -> list:
+    """fftgal_power_mixed_f32: interlaced P_l and wedges of every (x, y, z)
+    catalog of ``cats`` with its own volume V[c], grid Ng[c], box L[c] and bin
+    width dK[c] (scalars broadcast), in one call; a list of result dicts."""
+    n = len(cats)
+    arrs = [[np.ascontiguousarray(a, dtype=np.float32) for a in c] for c in cats]
+    ptr = [(C.c_void_p * n)(*[c[a].ctypes.data for c in arrs]) for a in range(3)]
+    Np = np.array([len(c[0]) for c in arrs], dtype=np.int64)
+
+    def vec(v, dt):
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=dt), (n,)))
+
+    Vs, Ls, dKs, Ngs = vec(V, np.float64), vec(L, np.float64), vec(dK, np.float64), vec(Ng, np.int32)
+    out = []
+    for c in range(n):
+        NK = lib().fftgal_nk(int(Ngs[c]), float(Ls[c]), float(dKs[c]))
+        out.append(dict(K=np.zeros(NK), N=np.zeros(NK, dtype=np.int64), P=np.zeros((NK, 4)),
+                        Kmu=np.zeros((NK, Nmu)), Nmu=np.zeros((NK, Nmu), dtype=np.int64),
+                        Pmu=np.zeros((NK, Nmu))))
+    tabs = [(C.c_void_p * n)(*[r[k].ctypes.data for r in out]) for k in ("K", "N", "P", "Kmu", "Nmu", "Pmu")]
+    l = _f64(los)
+    _check(lib().fftgal_power_mixed_f32(n, ptr[0], ptr[1], ptr[2], Np.ctypes.data_as(_lp), Vs.ctypes.data_as(_dp),
+                                        Ngs.ctypes.data_as(C.POINTER(C.c_int)), Ls.ctypes.data_as(_dp),
+                                        l.ctypes.data_as(_dp), dKs.ctypes.data_as(_dp), int(Nmu), *tabs))
+    return out
+
+
+def power_mixed_release():
+    _check(lib().fftgal_power_mixed_release())
 
 
 def nk(Ng: int, L: float, dK: float) -> int:

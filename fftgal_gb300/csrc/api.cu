@@ -26,6 +26,9 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace fg {
@@ -376,14 +379,19 @@ using namespace fg;
 // reference API: src/fft.h
 // ======================================================================================
 
-extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
-    fprintf(stderr, "fft_init() making a %d^3 grid in a %g^3 box\n", Ng, L);
+// a grid and its device state; host_view: allocate fft_t.f (the drop-in
+// API's host array), else f stays NULL and the grid runs with the lazy view.
+// Returns NULL with the status set on failure.
+static fft_t *grid_new(int Ng, double L, const char *wisdom, bool host_view, bool quiet) {
     if (Ng < 2) {
         set_error(ERR_ARG, "Ng must be >= 2");
-        die("fft_init()");
+        return nullptr;
     }
-    fft_t *self = (fft_t *)malloc(sizeof(fft_t));
-    if (!self) die("fft_init()");
+    fft_t *self = (fft_t *)calloc(1, sizeof(fft_t));
+    if (!self) {
+        set_error(ERR_NOMEM, "fft_t");
+        return nullptr;
+    }
     Grid *g = new Grid();
     self->x2k = g;
     self->k2x = nullptr;
@@ -393,40 +401,59 @@ extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
     self->Ng_pad = 2 * (Ng / 2 + 1);
     self->Ng3_pad = (long)Ng * Ng * self->Ng_pad;
     g->prec = env_precision();
-    g->view = env_view();
-    g->quiet = env_quiet();
+    g->view = host_view ? env_view() : FFTGAL_VIEW_LAZY;
+    g->quiet = quiet ? 1 : env_quiet();
     g->use_graphs = env_graphs();
     g->Ng = Ng;
     g->Ng_pad = self->Ng_pad;
     g->nh = Ng / 2 + 1;
     g->Ng3_pad = self->Ng3_pad;
     g->L = L;
-    FG_API(cuda_check(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking), "stream"), "fft_init()");
+    auto fail = [&]() -> fft_t * {
+        const int st = t_status;
+        char msg[sizeof(t_msg)];
+        memcpy(msg, t_msg, sizeof(msg));
+        fft_free(self);
+        t_status = st;
+        memcpy(t_msg, msg, sizeof(msg));
+        return nullptr;
+    };
+    if (cuda_check(cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking), "stream")) return fail();
     g->stream = g->own_stream;
-    // host view: pinned so the GPU converts straight into it
-    void *hv = nullptr;
-    if (cudaMallocHost(&hv, sizeof(double) * self->Ng3_pad) == cudaSuccess) {
-        g->pinned = true;
-    } else {
-        cudaGetLastError();
-        hv = malloc(sizeof(double) * self->Ng3_pad);
-        if (!hv) {
-            set_error(ERR_NOMEM, "host view of %ld doubles", self->Ng3_pad);
-            die("fft_init()");
+    if (host_view) {
+        // host view: pinned so the GPU converts straight into it
+        void *hv = nullptr;
+        if (cudaMallocHost(&hv, sizeof(double) * self->Ng3_pad) == cudaSuccess) {
+            g->pinned = true;
+        } else {
+            cudaGetLastError();
+            hv = malloc(sizeof(double) * self->Ng3_pad);
+            if (!hv) {
+                set_error(ERR_NOMEM, "host view of %ld doubles", self->Ng3_pad);
+                return fail();
+            }
         }
+        self->f = (double *)hv;
+        memset(self->f, 0, sizeof(double) * self->Ng3_pad);
     }
-    self->f = (double *)hv;
-    memset(self->f, 0, sizeof(double) * self->Ng3_pad);
-    FG_API(cuda_check(cudaMalloc(&g->d_f, (size_t)g->prec * self->Ng3_pad), "grid"), "fft_init()");
-    FG_API(cuda_check(cudaMemsetAsync(g->d_f, 0, (size_t)g->prec * self->Ng3_pad, g->stream), "grid"), "fft_init()");
-    FG_API(fft_plan_create(&g->fft, Ng, g->prec), "fft_init()");
-    FG_API(paint_tiling_create(&g->tiling, Ng), "fft_init()");
-    FG_API(cuda_check(cudaStreamSynchronize(g->stream), "init"), "fft_init()");
+    if (cuda_check(cudaMalloc(&g->d_f, (size_t)g->prec * self->Ng3_pad), "grid")) return fail();
+    if (cuda_check(cudaMemsetAsync(g->d_f, 0, (size_t)g->prec * self->Ng3_pad, g->stream), "grid")) return fail();
+    if (fft_plan_create(&g->fft, Ng, g->prec)) return fail();
+    if (paint_tiling_create(&g->tiling, Ng)) return fail();
+    if (cuda_check(cudaStreamSynchronize(g->stream), "init")) return fail();
     if (!wisdom || !strcmp(wisdom, "FFTW_ESTIMATE")) {
-        fprintf(stderr, "fft_init() using built-in GPU plans (%s grid)\n", g->prec == 4 ? "FP32" : "FP64");
-    } else {
-        FG_API(plan_resolve(&g->fft, g->d_f, g->stream, wisdom, false, &g->plan_source, g->plan_ms), "fft_init()");
+        if (!g->quiet)
+            fprintf(stderr, "fft_init() using built-in GPU plans (%s grid)\n", g->prec == 4 ? "FP32" : "FP64");
+    } else if (plan_resolve(&g->fft, g->d_f, g->stream, wisdom, g->quiet != 0, &g->plan_source, g->plan_ms)) {
+        return fail();
     }
+    return self;
+}
+
+extern "C" fft_t *fft_init(int Ng, double L, char *wisdom) {
+    fprintf(stderr, "fft_init() making a %d^3 grid in a %g^3 box\n", Ng, L);
+    fft_t *self = grid_new(Ng, L, wisdom, true, false);
+    if (!self) die("fft_init()");
     return self;
 }
 
@@ -462,7 +489,7 @@ extern "C" void fft_free(fft_t *self) {
             if (g->pinned)
                 cudaFreeHost(self->f);
             else
-                free(self->f);
+                free(self->f);  // NULL for grids without a host view
             delete g;
         }
     }
@@ -1361,7 +1388,7 @@ static int power_batch_graph(fft_t *grid, int ncat, const float *const *x, const
         FG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->buf_free[b], 0));
         const float *src[3] = {x[c], y[c], z[c]};
         for (int a = 0; a < 3; ++a)
-            FG_CUDA(cudaMemcpyAsync(d + (size_t)a * capNp, src[a], sizeof(float) * Np[c], cudaMemcpyHostToDevice,
+            FG_CUDA(cudaMemcpyAsync(d + (size_t)a * capNp, src[a], sizeof(float) * Np[c], cudaMemcpyDefault,
                                     g->copy_stream));
         FG_CUDA(cudaMemcpyAsync(g->d_scal + b, g->h_scal + c, sizeof(DevScalars), cudaMemcpyHostToDevice,
                                 g->copy_stream));
@@ -1450,7 +1477,7 @@ extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const 
         FG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->buf_free[b], 0));
         const float *src[3] = {x[c], y[c], z[c]};
         for (int a = 0; a < 3; ++a)
-            FG_CUDA(cudaMemcpyAsync(d + (size_t)a * Np[c], src[a], sizeof(float) * Np[c], cudaMemcpyHostToDevice,
+            FG_CUDA(cudaMemcpyAsync(d + (size_t)a * Np[c], src[a], sizeof(float) * Np[c], cudaMemcpyDefault,
                                     g->copy_stream));
         FG_CUDA(cudaEventRecord(g->up_done[b], g->copy_stream));
         return OK;
@@ -1470,6 +1497,98 @@ extern "C" int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const 
         FG_CUDA(cudaEventRecord(g->buf_free[b], g->stream));
     }
     FG_CUDA(cudaStreamSynchronize(g->copy_stream));
+    return OK;
+}
+
+// ---- catalogs of mixed grid sizes and boxes in one call ----------------------------------
+// Grids kept between calls, one per (device, Ng, box length): device state
+// only (no host view), released by fftgal_power_mixed_release.
+static std::mutex g_mixed_mutex;
+static std::map<std::tuple<int, int, double>, fft_t *> g_mixed_grids;
+
+extern "C" int fftgal_power_mixed_release(void) {
+    std::lock_guard<std::mutex> lock(g_mixed_mutex);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (auto it = g_mixed_grids.begin(); it != g_mixed_grids.end();) {
+        if (std::get<0>(it->first) == dev) {
+            fft_free(it->second);
+            it = g_mixed_grids.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    return OK;
+}
+
+extern "C" int fftgal_power_mixed_f32(int ncat, const float *const *x, const float *const *y, const float *const *z,
+                                      const long *Np, const double *V, const int *Ng, const double *L,
+                                      const double los[3], const double *dK, int Nmu, double *const *K,
+                                      long *const *N, double *const *Pl, double *const *Kmu, long *const *Nmu_count,
+                                      double *const *Pmu) {
+    if (ncat < 0 || (ncat > 0 && (!x || !y || !z || !Np || !V || !Ng || !L || !dK || !los)))
+        return set_error(ERR_ARG, "fftgal_power_mixed_f32: bad arguments");
+    if (ncat == 0) return OK;
+    int dev = 0;
+    FG_CUDA(cudaGetDevice(&dev));
+    // groups of catalogs with the same (Ng, box, dK), in order of first appearance
+    std::vector<std::tuple<int, double, double>> keys;
+    std::vector<std::vector<int>> members;
+    for (int c = 0; c < ncat; ++c) {
+        if (Ng[c] < 2 || !(L[c] > 0) || !(dK[c] > 0))
+            return set_error(ERR_ARG, "fftgal_power_mixed_f32: catalog %d: bad Ng, L or dK", c);
+        const auto key = std::make_tuple(Ng[c], L[c], dK[c]);
+        size_t q = 0;
+        while (q < keys.size() && keys[q] != key) ++q;
+        if (q == keys.size()) {
+            keys.push_back(key);
+            members.emplace_back();
+        }
+        members[q].push_back(c);
+    }
+    std::lock_guard<std::mutex> lock(g_mixed_mutex);
+    for (size_t q = 0; q < keys.size(); ++q) {
+        const int ng = std::get<0>(keys[q]);
+        const double box = std::get<1>(keys[q]), dk = std::get<2>(keys[q]);
+        fft_t *&grid = g_mixed_grids[std::make_tuple(dev, ng, box)];
+        if (!grid) {
+            grid = grid_new(ng, box, "FFTW_ESTIMATE", false, true);
+            if (!grid) {
+                g_mixed_grids.erase(std::make_tuple(dev, ng, box));
+                return t_status ? t_status : ERR_CUDA;
+            }
+        }
+        if (G(grid)->prec != 4) return set_error(ERR_STATE, "fftgal_power_mixed_f32 needs FP32 grids");
+        const std::vector<int> &m = members[q];
+        const int n = (int)m.size();
+        const int NK = fftgal_nk(ng, box, dk);
+        if (NK < 1) return set_error(ERR_ARG, "fftgal_power_mixed_f32: bad dK for catalog %d", m[0]);
+        std::vector<const float *> gx(n), gy(n), gz(n);
+        std::vector<long> gn(n);
+        std::vector<double> gv(n);
+        for (int i = 0; i < n; ++i) {
+            gx[i] = x[m[i]];
+            gy[i] = y[m[i]];
+            gz[i] = z[m[i]];
+            gn[i] = Np[m[i]];
+            gv[i] = V[m[i]];
+        }
+        std::vector<double> bK((size_t)n * NK), bPl((size_t)n * NK * 4), bKm((size_t)n * NK * Nmu),
+            bPm((size_t)n * NK * Nmu);
+        std::vector<long> bN((size_t)n * NK), bNm((size_t)n * NK * Nmu);
+        FG_TRY(fftgal_power_batch_f32(grid, n, gx.data(), gy.data(), gz.data(), gn.data(), gv.data(), los, dk, Nmu,
+                                      bK.data(), bN.data(), bPl.data(), bKm.data(), bNm.data(), bPm.data()));
+        for (int i = 0; i < n; ++i) {
+            const int c = m[i];
+            const size_t o1 = (size_t)i * NK, o4 = o1 * 4, om = o1 * Nmu;
+            if (K && K[c]) memcpy(K[c], &bK[o1], sizeof(double) * NK);
+            if (N && N[c]) memcpy(N[c], &bN[o1], sizeof(long) * NK);
+            if (Pl && Pl[c]) memcpy(Pl[c], &bPl[o4], sizeof(double) * 4 * NK);
+            if (Kmu && Kmu[c]) memcpy(Kmu[c], &bKm[om], sizeof(double) * Nmu * NK);
+            if (Nmu_count && Nmu_count[c]) memcpy(Nmu_count[c], &bNm[om], sizeof(long) * Nmu * NK);
+            if (Pmu && Pmu[c]) memcpy(Pmu[c], &bPm[om], sizeof(double) * Nmu * NK);
+        }
+    }
     return OK;
 }
 

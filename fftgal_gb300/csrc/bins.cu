@@ -20,6 +20,7 @@
 #include "binmath.cuh"
 
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 #include <vector>
 
@@ -292,7 +293,7 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
 // slowest, so a run crosses the fewest k-bin edges (about 0.3 per mode,
 // against 0.55 along a fixed axis).  A thread keeps the run's sums in
 // registers and adds them to the CTA's FP32 shared accumulators when the bin
-// (or the wedge) changes; every kFoldBlocks blocks the CTA adds its FP32
+// (or the wedge) changes; every `fold` blocks the CTA adds its FP32
 // sums to the FP64 global accumulators.
 //   MODE 0: the grid holds P in F_Re (after P()).
 //   MODE 1: the grid holds delta; P = |delta|^2 Vinv - Pshot.
@@ -306,7 +307,15 @@ bin_power_kernel(BinDev d, const T *__restrict__ f, T Vinv, T Pshot,
 //           Ng = 1024).
 constexpr int kSlabI = 16, kSlabJ = 16, kSlabK = 32, kSlabRow = 33;
 constexpr int kSlabThreads = 512;  // one warp per slab of a block
-constexpr int kFoldBlocks = 8;
+// blocks between folds of the FP32 sums into FP64: FFTGAL_BIN_FOLD, default 8
+static int fold_blocks() {
+    static const int v = [] {
+        const char *e = getenv("FFTGAL_BIN_FOLD");
+        const int n = e ? atoi(e) : 0;
+        return n >= 1 && n <= 1024 ? n : 8;
+    }();
+    return v;
+}
 
 struct SlabFinish {
     float2 *A = nullptr;
@@ -319,7 +328,8 @@ struct SlabFinish {
 template <int MODE>
 __global__ void __launch_bounds__(kSlabThreads, 3)
 bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, float Vinv, float Pshot,
-                      const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, const DevScalars *__restrict__ ds) {
+                      const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, const DevScalars *__restrict__ ds,
+                      int fold) {
     if (ds) {
         Vinv = ds->Vinv;
         Pshot = ds->Pshot;
@@ -404,7 +414,7 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
             run.finish(d, acc32);
         }
         __syncwarp();
-        if (++since_fold == kFoldBlocks) {
+        if (++since_fold == fold) {
             since_fold = 0;
             __syncthreads();
             bin_fold(acc32, gacc, NK, NQ);
@@ -485,7 +495,7 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
         FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                                      (int)smem));                                                           \
         bin_power_slab_kernel<M><<<(unsigned)nb, kSlabThreads, smem, st>>>(d, fv, sf, (float)Vinv, (float)Pshot, \
-                                                                         g->d_thr, g->d_acc, ds);           \
+                                                                         g->d_thr, g->d_acc, ds, fold_blocks()); \
     } while (0)
         if (mode == 0)
             FG_SLAB_LAUNCH(0);

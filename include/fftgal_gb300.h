@@ -117,7 +117,8 @@ int fftgal_dl_sub(fft_t *grid, int sphere, int Nsub, int nlos, const double *los
                   double *DeltaL);
 
 /* fftgal_power_f32 over a list of ncat catalogs with FP32 positions in host
- * memory (x[c], y[c], z[c], Np[c] particles, volume V[c]): while catalog c is
+ * (or device) memory (x[c], y[c], z[c], Np[c] particles, volume V[c]): while
+ * catalog c is
  * painted and transformed, catalog c + 1 is copied to the GPU on a second
  * stream, so with page-locked host arrays the host-to-device copies hide
  * behind the computation.  Outputs are the fftgal_power_f32 outputs of each
@@ -136,6 +137,27 @@ int fftgal_power_batch_f32(fft_t *grid, int ncat, const float *const *x, const f
                            const float *const *z, const long *Np, const double *V,
                            const double los[3], double dK, int Nmu, double *K, long *N,
                            double *Pl, double *Kmu, long *Nmu_count, double *Pmu);
+
+/* Interlaced power spectra of a list of catalogs of mixed grid sizes, box
+ * lengths (fold factors: L[c] = L_box / fold, src/app/P.c:35-36) and bin
+ * widths in one call, e.g. a covariance set of mocks with uneven particle
+ * counts.  Catalog c: FP32 positions x[c], y[c], z[c] (host or device),
+ * Np[c] particles, volume V[c], grid Ng[c], box L[c], bin width dK[c]; its
+ * outputs go to K[c][NK_c], N[c][NK_c], Pl[c][NK_c*4], Kmu[c], Nmu_count[c],
+ * Pmu[c][NK_c*Nmu] with NK_c = fftgal_nk(Ng[c], L[c], dK[c]) (any array of
+ * pointers, or any pointer in it, may be NULL).  Catalogs with the same
+ * (Ng, L, dK) run together through fftgal_power_batch_f32 (uploads overlapped,
+ * each catalog one captured graph launch) on an FP32 grid kept per (device,
+ * Ng, L) between calls with device memory only, released by
+ * fftgal_power_mixed_release.  Results equal fftgal_power_f32 on each
+ * catalog.  No counterpart in the reference (its job scripts run one process
+ * per mock, src/app/job_P.sh:22-26).  Not thread-safe with itself. */
+int fftgal_power_mixed_f32(int ncat, const float *const *x, const float *const *y, const float *const *z,
+                           const long *Np, const double *V, const int *Ng, const double *L,
+                           const double los[3], const double *dK, int Nmu, double *const *K,
+                           long *const *N, double *const *Pl, double *const *Kmu, long *const *Nmu_count,
+                           double *const *Pmu);
+int fftgal_power_mixed_release(void);
 
 /* fftgal_power_f32 without interlacing: one paint, r2c, PCS deconvolution,
  * multipoles and wedges -- the sequence fft_p2g(offset 0) -> fft_x2k(0) ->
