@@ -112,6 +112,7 @@ SIGNATURES = {
     "fftgal_alias_envelope": (C.c_double, [C.c_double]),
     "fftgal_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
     "fftgal_plan_autotune": (C.c_int, [C.c_void_p, _dp]),
+    "fftgal_launch_shapes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp]),
     "fftgal_plan_lookup": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "fftgal_plan_store": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), _dp,
                                     C.c_char_p]),
@@ -345,6 +346,15 @@ class Grid:
         ms = np.zeros(3)
         _check(lib().fftgal_plan_autotune(self.p, ms.ctypes.data_as(_dp)))
         return ms
+
+    def launch_shapes(self) -> dict:
+        """fftgal_launch_shapes: paint CTAs per SM, binning CTAs per SM and fold
+        period (0: built-in), where they came from, measured times."""
+        sh = (C.c_int * 3)()
+        src = C.c_int(0)
+        ms = np.zeros(2)
+        _check(lib().fftgal_launch_shapes(self.p, sh, C.byref(src), ms.ctypes.data_as(_dp)))
+        return dict(paint_cta=sh[0], bin_cta=sh[1], bin_fold=sh[2], source=src.value, ms=ms)
 
     def set_stream(self, stream_ptr: int | None):
         """Run the grid's work on a CUDA stream: None for the library's own

@@ -118,6 +118,9 @@ struct Grid {
     cudaEvent_t ev[kStages + 1] = {};
     double stage_ms[kStages + 1] = {};
     int plan_source = FFTGAL_PLAN_BUILTIN;
+    LaunchTune launch;  // paint / binning launch shapes (0: built-in)
+    int launch_source = FFTGAL_PLAN_BUILTIN;
+    double launch_ms[2] = {0, 0};
     double plan_ms[3] = {0, 0, 0};
     // graph-captured batches: one executable graph per upload buffer, the
     // per-catalog scalars it reads (device, one block per buffer; pinned
@@ -368,7 +371,180 @@ static BinGeometry *geometry(Grid *g, const BinSpec &s) {
     BinGeometry &c = g->geo[g->geo_next];
     g->geo_next = (g->geo_next + 1) % kGeoCache;
     if (bin_geometry_build(&c, s, g->stream) != OK) return nullptr;
+    c.cta_per_sm = g->launch.bin_cta;
+    c.fold = g->launch.bin_fold;
     return &c;
+}
+
+// ---- launch shapes of the paint and binning kernels (autotuned) ----------------------------
+// uniform FP32 positions in [0, L) from the splitmix64 stream of `seed`
+__global__ void tune_uniform_kernel(float *x, long n, float L, unsigned long long seed) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const float u = (float)(z >> 40) * (1.0f / 16777216.0f);  // 24 bits: [0, 1)
+        x[i] = L * u < L ? L * u : 0.f;
+    }
+}
+
+// median of 3 timed runs after one untimed, CUDA events on st
+template <typename F>
+static int median_ms(cudaStream_t st, F run, double *ms) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FG_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_check(ce, "tune events");
+    }
+    int rc = run();
+    float t[3] = {0, 0, 0};
+    for (int r = 0; r < 3 && rc == OK; ++r) {
+        rc = cuda_check(cudaEventRecord(e0, st), "tune");
+        if (rc == OK) rc = run();
+        if (rc == OK) rc = cuda_check(cudaEventRecord(e1, st), "tune");
+        if (rc == OK) rc = cuda_check(cudaEventSynchronize(e1), "tune");
+        if (rc == OK) rc = cuda_check(cudaEventElapsedTime(&t[r], e0, e1), "tune");
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    FG_TRY(rc);
+    std::sort(t, t + 3);
+    *ms = t[1];
+    return OK;
+}
+
+static std::mutex g_launch_mu;
+static std::map<std::tuple<int, int, int>, LaunchTune> g_launch_cache;
+
+// The counterpart of plan_resolve for the paint and binning launch shapes of
+// an FP32 grid with the two-level FFT: the plan file's launch line for this
+// device and Ng, else this process's earlier measurement, else timing every
+// shape (binning: 1-3 CTAs per SM x fold every 8 or 32 blocks on zero grids;
+// tile paint: 1 or 2 persistent CTAs per SM on a uniform catalog of Ng^3/10
+// particles) and writing the line.  The built-in shape stays unless another
+// is more than 2 % faster.  The grids are left zeroed.
+static int tune_launch(fft_t *self, const char *path) {
+    Grid *g = G(self);
+    const int Ng = self->Ng;
+    if (g->prec != 4 || !fft2_supported(Ng, 4)) return OK;
+    int cc = 0, sms = 0;
+    char name[256];
+    FG_TRY(plan_device_key(&cc, &sms, name, sizeof(name)));
+    LaunchTune t;
+    const auto key = std::make_tuple(cc, sms, Ng);
+    if (launch_lookup(path, cc, sms, Ng, &t)) {
+        g->launch_source = FFTGAL_PLAN_FILE;
+    } else {
+        bool cached = false;
+        {
+            std::lock_guard<std::mutex> lk(g_launch_mu);
+            auto it = g_launch_cache.find(key);
+            if (it != g_launch_cache.end()) {
+                t = it->second;
+                cached = true;
+            }
+        }
+        if (cached) {
+            g->launch_source = FFTGAL_PLAN_CACHE;
+        } else {
+            cudaStream_t st = g->stream;
+            FG_TRY(ensure_aux(g));
+            FG_TRY(ensure_tables(g));
+            const size_t gb = (size_t)4 * self->Ng3_pad;
+            FG_CUDA(cudaMemsetAsync(g->d_f, 0, gb, st));
+            FG_CUDA(cudaMemsetAsync(g->d_aux, 0, gb, st));
+            // binning: the interlaced finish + binning of fftgal_power_f32 (lazy view)
+            const double los[3] = {0, 0, 1};
+            BinSpec bs;
+            FG_TRY(bin_spec_init(&bs, Ng, self->L, 2 * M_PI / self->L, los, 3));
+            BinGeometry *geo = geometry(g, bs);
+            if (!geo) return t_status ? t_status : ERR_CUDA;
+            BinFinish fin;
+            fin.A = g->d_f;
+            fin.B = g->d_aux;
+            fin.ph32 = dual_tab32(g);
+            fin.w32 = winv_tab32(g);
+            fin.scale = 0.5 * H3_of(g);
+            double best_b = 0, def_b = 0;
+            t.bin_cta = 3;
+            t.bin_fold = 8;
+            for (int cta = 3; cta >= 1; --cta)
+                for (int fold : {8, 32}) {
+                    geo->cta_per_sm = cta;
+                    geo->fold = fold;
+                    double ms = 0;
+                    FG_TRY(median_ms(st, [&]() { return bin_power_launch(geo, 5, 1.0, 0.0, st, &fin, nullptr); }, &ms));
+                    if (cta == 3 && fold == 8) {
+                        def_b = best_b = ms;
+                    } else if (ms < best_b && ms < 0.98 * def_b) {
+                        best_b = ms;
+                        t.bin_cta = cta;
+                        t.bin_fold = fold;
+                    }
+                }
+            geo->cta_per_sm = t.bin_cta;
+            geo->fold = t.bin_fold;
+            // tile paint of both interlacing grids on a uniform catalog
+            long Np = (long)Ng * Ng * Ng / 10;
+            Np = Np < 100000 ? 100000 : (Np > 200000000 ? 200000000 : Np);
+            float *pos = nullptr;
+            FG_CUDA(cudaMalloc(&pos, sizeof(float) * 3 * (size_t)Np));
+            for (int a = 0; a < 3; ++a)
+                tune_uniform_kernel<<<num_sms() * 8, 256, 0, st>>>(pos + (size_t)a * Np, Np, (float)self->L,
+                                                                   0x5EEDull + (unsigned long long)a);
+            note_launches(3);
+            PaintGridSpec spec[2];
+            spec[0].out = g->d_f;
+            spec[1].out = g->d_aux;
+            for (int a = 0; a < 3; ++a) {
+                spec[0].offset[a] = 0;
+                spec[1].offset[a] = remainder(0.5, Ng);
+            }
+            double best_p = 0, def_p = 0;
+            t.paint_cta = 2;
+            int rc = cuda_check(cudaGetLastError(), "tune catalog");
+            for (int cta = 2; cta >= 1 && rc == OK; --cta) {
+                g->tiling.cta_per_sm = cta;
+                double ms = 0;
+                rc = median_ms(st, [&]() {
+                    return paint(&g->tiling, &g->scratch, 4, pos, pos + Np, pos + 2 * (size_t)Np, 4, Np,
+                                 Ng / self->L, spec, 2, st);
+                }, &ms);
+                if (rc != OK) break;
+                if (cta == 2) {
+                    def_p = best_p = ms;
+                } else if (ms < 0.98 * def_p) {
+                    best_p = ms;
+                    t.paint_cta = cta;
+                }
+            }
+            cudaFree(pos);
+            FG_TRY(rc);
+            FG_CUDA(cudaMemsetAsync(g->d_f, 0, gb, st));
+            FG_CUDA(cudaMemsetAsync(g->d_aux, 0, gb, st));
+            FG_CUDA(cudaStreamSynchronize(st));
+            g->launch_ms[0] = best_p;
+            g->launch_ms[1] = best_b;
+            g->launch_source = FFTGAL_PLAN_MEASURED;
+            {
+                std::lock_guard<std::mutex> lk(g_launch_mu);
+                g_launch_cache[key] = t;
+            }
+        }
+        if (launch_store(path, cc, sms, Ng, t, g->launch_ms, name) != OK)
+            fprintf(stderr, "fft_init() could not export the launch shapes to %s: %s\n", path, fftgal_last_error());
+    }
+    g->launch = t;
+    g->tiling.cta_per_sm = t.paint_cta;
+    for (auto &c : g->geo)
+        if (c.valid) {
+            c.cta_per_sm = t.bin_cta;
+            c.fold = t.bin_fold;
+        }
+    return OK;
 }
 
 }  // namespace fg
@@ -444,7 +620,8 @@ static fft_t *grid_new(int Ng, double L, const char *wisdom, bool host_view, boo
     if (!wisdom || !strcmp(wisdom, "FFTW_ESTIMATE")) {
         if (!g->quiet)
             fprintf(stderr, "fft_init() using built-in GPU plans (%s grid)\n", g->prec == 4 ? "FP32" : "FP64");
-    } else if (plan_resolve(&g->fft, g->d_f, g->stream, wisdom, g->quiet != 0, &g->plan_source, g->plan_ms)) {
+    } else if (plan_resolve(&g->fft, g->d_f, g->stream, wisdom, g->quiet != 0, &g->plan_source, g->plan_ms) ||
+               tune_launch(self, wisdom)) {
         return fail();
     }
     return self;
@@ -933,6 +1110,22 @@ extern "C" int fftgal_fft_columns_f32(int N, void *data, int ncols, long es, lon
     if (rc == OK) rc = cuda_check(cudaStreamSynchronize(st), "fftgal_fft_columns_f32");
     fft_plan_destroy(&p);
     return rc;
+}
+
+extern "C" int fftgal_launch_shapes(fft_t *grid, int shapes[3], int *source, double ms[2]) {
+    if (!grid) return set_error(ERR_ARG, "null grid");
+    Grid *g = G(grid);
+    if (shapes) {
+        shapes[0] = g->launch.paint_cta > 0 ? g->launch.paint_cta : 2;
+        shapes[1] = g->launch.bin_cta > 0 ? g->launch.bin_cta : 3;
+        shapes[2] = g->launch.bin_fold > 0 ? g->launch.bin_fold : 0;
+    }
+    if (source) *source = g->launch_source;
+    if (ms) {
+        ms[0] = g->launch_ms[0];
+        ms[1] = g->launch_ms[1];
+    }
+    return OK;
 }
 
 extern "C" int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms[3]) {

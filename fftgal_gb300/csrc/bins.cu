@@ -478,6 +478,7 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
     if (prec == 4) {
         int per_sm = (int)((224 * 1024) / (smem + 1024));
         per_sm = per_sm < 1 ? 1 : (per_sm > 3 ? 3 : per_sm);
+        if (g->cta_per_sm > 0 && g->cta_per_sm < per_sm) per_sm = g->cta_per_sm;  // tuned shape
         const long nblk = ceil_div(s.Ng, kSlabI) * ceil_div(s.Ng, kSlabJ) * ceil_div(s.Ng / 2 + 1, kSlabK);
         long nb = (long)num_sms() * per_sm;
         if (nb > nblk) nb = nblk;
@@ -495,7 +496,7 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
         FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
                                      (int)smem));                                                           \
         bin_power_slab_kernel<M><<<(unsigned)nb, kSlabThreads, smem, st>>>(d, fv, sf, (float)Vinv, (float)Pshot, \
-                                                                         g->d_thr, g->d_acc, ds, fold_blocks()); \
+                                                                         g->d_thr, g->d_acc, ds, g->fold > 0 ? g->fold : fold_blocks()); \
     } while (0)
         if (mode == 0)
             FG_SLAB_LAUNCH(0);

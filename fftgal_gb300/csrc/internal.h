@@ -112,6 +112,17 @@ int fft2_autotune(FftPlan *p, void *grid, cudaStream_t s, double ms[3]);
 // size, else the in-process cache, else fft2_autotune on `grid`; writes the
 // entry back to `path`.  *source: FFTGAL_PLAN_*; ms: measured times or 0.
 int plan_resolve(FftPlan *p, void *grid, cudaStream_t s, const char *path, bool quiet, int *source, double ms[3]);
+// Launch shapes of the paint and binning kernels of an FP32 grid, kept in the
+// same plan file on lines of their own ("fftgal_gb300-launch 1 ...") per
+// (compute capability, SM count, Ng).  0 = built-in.
+struct LaunchTune {
+    int paint_cta = 0;  // persistent tile-paint CTAs per SM
+    int bin_cta = 0;    // binning CTAs per SM
+    int bin_fold = 0;   // binning blocks between folds
+};
+int plan_device_key(int *cc, int *sms, char *name, size_t len);
+int launch_lookup(const char *path, int cc, int sms, int Ng, LaunchTune *t);
+int launch_store(const char *path, int cc, int sms, int Ng, const LaunchTune &t, const double ms[2], const char *dev);
 
 // ---- paint -----------------------------------------------------------------
 struct PaintTiling {
@@ -121,6 +132,7 @@ struct PaintTiling {
     int *d_tables = nullptr;      // device, per axis a: tile_of[Ng], then start[nt[a]+1]
     int tab_off[3] = {0, 0, 0};   // offset of axis a's tables in d_tables
     long nkeys = 0;               // nt0*nt1*nt2 * 27
+    int cta_per_sm = 0;           // persistent FP32 tile-paint CTAs per SM (1 or 2; 0: built-in 2)
 };
 
 struct PaintScratch {
@@ -218,6 +230,8 @@ struct BinGeometry {               // data-independent part, cached
     double *d_acc = nullptr;      // device accumulators (per call)
     size_t acc_len = 0;
     int bad = 0;
+    // FP32 binning launch shape (0: built-in): CTAs per SM, blocks between folds
+    int cta_per_sm = 0, fold = 0;
 };
 
 int bin_spec_init(BinSpec *b, int Ng, double L, double dK, const double los_hat[3], int Nmu);

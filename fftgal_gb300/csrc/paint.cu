@@ -1133,7 +1133,7 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
         const size_t smem = kAccBytes + sizeof(StageBuf) * (kPaintThreads / 32) + sizeof(uint32_t) * kBlkN;
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        unsigned nb = (unsigned)(2 * num_sms());
+        unsigned nb = (unsigned)((t->cta_per_sm == 1 ? 1 : 2) * num_sms());
         nb = nb < ntiles ? nb : ntiles;
         if (ngrids == 1)
             paint_coop_kernel<1><<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);

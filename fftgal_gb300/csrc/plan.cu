@@ -7,6 +7,10 @@
 //
 //   fftgal_gb300-plan 1 cc=103 sms=152 Ng=1024 prec=4 kR=4 jlogC=3 ilogC=4 ms=4.010,4.290,4.660 dev=<name>
 //
+// and, for FP32 grids, the launch shapes of the tile paint (persistent CTAs
+// per SM) and of the finish + binning kernel (CTAs per SM, blocks between
+// the folds of its FP32 sums) on lines of their own (launch_store).
+//
 // Other lines of the file are kept as they are.  Entries measured in this
 // process are also kept in memory, so a second grid of the same size is not
 // measured again.
@@ -83,20 +87,14 @@ int plan_lookup(const char *path, int cc, int sms, int Ng, int prec, int tun[3])
     return found;
 }
 
-int plan_store(const char *path, int cc, int sms, int Ng, int prec, const int tun[3], const double ms[3],
-               const char *dev) {
+// the file with every line for which `same` holds replaced by `line`
+template <typename F>
+static int replace_line(const char *path, F same, const char *line) {
     std::vector<std::string> lines, keep;
     read_lines(path, &lines);
-    for (const auto &l : lines) {
-        int c, s, n, p, t[3];
-        if (parse_line(l.c_str(), &c, &s, &n, &p, t) && c == cc && s == sms && n == Ng && p == prec) continue;
-        keep.push_back(l);
-    }
-    char buf[512];
-    snprintf(buf, sizeof(buf), "%scc=%d sms=%d Ng=%d prec=%d kR=%d jlogC=%d ilogC=%d ms=%.3f,%.3f,%.3f dev=%s", kTag,
-             cc, sms, Ng, prec, tun[0], tun[1], tun[2], ms ? ms[0] : 0.0, ms ? ms[1] : 0.0, ms ? ms[2] : 0.0,
-             dev ? dev : "");
-    keep.push_back(buf);
+    for (const auto &l : lines)
+        if (!same(l.c_str())) keep.push_back(l);
+    keep.push_back(line);
     // write beside the target and rename, so a reader never sees half a file
     std::string tmp = std::string(path) + ".tmp" + std::to_string((long)getpid());
     FILE *fp = fopen(tmp.c_str(), "w");
@@ -109,6 +107,63 @@ int plan_store(const char *path, int cc, int sms, int Ng, int prec, const int tu
         return set_error(ERR_IO, "cannot write plan file %s", path);
     }
     return OK;
+}
+
+int plan_store(const char *path, int cc, int sms, int Ng, int prec, const int tun[3], const double ms[3],
+               const char *dev) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%scc=%d sms=%d Ng=%d prec=%d kR=%d jlogC=%d ilogC=%d ms=%.3f,%.3f,%.3f dev=%s", kTag,
+             cc, sms, Ng, prec, tun[0], tun[1], tun[2], ms ? ms[0] : 0.0, ms ? ms[1] : 0.0, ms ? ms[2] : 0.0,
+             dev ? dev : "");
+    return replace_line(path, [&](const char *l) {
+        int c, s, n, p, t[3];
+        return parse_line(l, &c, &s, &n, &p, t) && c == cc && s == sms && n == Ng && p == prec;
+    }, buf);
+}
+
+// ---- launch shapes of the paint and binning kernels ------------------------------------------
+//   fftgal_gb300-launch 1 cc=103 sms=152 Ng=1024 paint_cta=2 bin_cta=3 bin_fold=8 ms=11.8,5.1 dev=<name>
+static const char kLTag[] = "fftgal_gb300-launch 1 ";
+
+static bool parse_launch(const char *line, int *cc, int *sms, int *Ng, LaunchTune *t) {
+    if (strncmp(line, kLTag, sizeof(kLTag) - 1)) return false;
+    int c, s, n, a, b, f;
+    if (sscanf(line + sizeof(kLTag) - 1, "cc=%d sms=%d Ng=%d paint_cta=%d bin_cta=%d bin_fold=%d", &c, &s, &n, &a,
+               &b, &f) != 6)
+        return false;
+    *cc = c;
+    *sms = s;
+    *Ng = n;
+    t->paint_cta = a;
+    t->bin_cta = b;
+    t->bin_fold = f;
+    return true;
+}
+
+int launch_lookup(const char *path, int cc, int sms, int Ng, LaunchTune *t) {
+    std::vector<std::string> lines;
+    if (!read_lines(path, &lines)) return 0;
+    int found = 0;
+    for (const auto &l : lines) {  // the last matching line wins
+        int c, s, n;
+        LaunchTune u;
+        if (parse_launch(l.c_str(), &c, &s, &n, &u) && c == cc && s == sms && n == Ng) {
+            *t = u;
+            found = 1;
+        }
+    }
+    return found;
+}
+
+int launch_store(const char *path, int cc, int sms, int Ng, const LaunchTune &t, const double ms[2], const char *dev) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%scc=%d sms=%d Ng=%d paint_cta=%d bin_cta=%d bin_fold=%d ms=%.3f,%.3f dev=%s", kLTag, cc,
+             sms, Ng, t.paint_cta, t.bin_cta, t.bin_fold, ms ? ms[0] : 0.0, ms ? ms[1] : 0.0, dev ? dev : "");
+    return replace_line(path, [&](const char *l) {
+        int c, s, n;
+        LaunchTune u;
+        return parse_launch(l, &c, &s, &n, &u) && c == cc && s == sms && n == Ng;
+    }, buf);
 }
 
 struct DevKey {
@@ -124,6 +179,15 @@ static int device_key(DevKey *k) {
     k->cc = prop.major * 10 + prop.minor;
     k->sms = prop.multiProcessorCount;
     snprintf(k->name, sizeof(k->name), "%s", prop.name);
+    return OK;
+}
+
+int plan_device_key(int *cc, int *sms, char *name, size_t len) {
+    DevKey k;
+    FG_TRY(device_key(&k));
+    *cc = k.cc;
+    *sms = k.sms;
+    if (name && len) snprintf(name, len, "%s", k.name);
     return OK;
 }
 

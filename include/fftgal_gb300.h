@@ -214,6 +214,17 @@ double fftgal_alias_envelope(double u);
 int fftgal_plan_info(fft_t *grid, int tune[3], int *source, double ms[3]);
 /* measure now (clears the grid) and keep the fastest shapes on this grid */
 int fftgal_plan_autotune(fft_t *grid, double ms[3]);
+/* Launch shapes of the tile paint and of the finish + binning kernel of an
+ * FP32 grid (power-of-two Ng): shapes[0] = persistent paint CTAs per SM
+ * (1 or 2), shapes[1] = binning CTAs per SM (1-3, fewer when its shared
+ * accumulators do not fit), shapes[2] = binning blocks between the folds of
+ * its FP32 sums into FP64 (0: built-in, 8 or FFTGAL_BIN_FOLD).  With a plan
+ * file, fft_init imports them from the file's "fftgal_gb300-launch" line for
+ * this device and Ng, or times every shape (binning on zero grids, the paint
+ * on a uniform catalog of Ng^3/10 particles; built-in kept unless another is
+ * more than 2 % faster) and writes the line; `source` as fftgal_plan_info,
+ * ms = the chosen paint and binning times (0 unless measured). */
+int fftgal_launch_shapes(fft_t *grid, int shapes[3], int *source, double ms[2]);
 /* in-place unnormalised FFTs of length N (a power of two from 4 to 2048) along
  * strided columns of complex FP32 data in GPU memory, with the kernels of the
  * grid's j and i passes: element n of column c (c < ncols) of batch b

@@ -471,3 +471,32 @@ def test_empty_and_wrapped_catalogs(fg, oracle_lib, prec, rel):
                 assert np.isnan(np.array(g.f)).all()
             else:
                 grid_close(np.array(g.f), np.array(o.f), rel)
+
+
+@pytest.mark.parametrize("n_clump", [200_000, 3_000_000])
+def test_dense_clump_fixed_point_scale(fg, oracle_lib, n_clump):
+    """A clump of n_clump particles inside one cell on top of 1e5 uniform ones:
+    the tile's 32-bit fixed-point sums then take a per-tile scale of about
+    log2(1.45e10 / n) fraction bits (16 and 12 here, against 21-23 for
+    uniform catalogs).  The painted real-space grid stays within 2e-5 of the
+    FP64 oracle's (scale: its largest cell), and P_0,2,4 within the parity
+    bound."""
+    Ng, L = 32, 100.0
+    rng = np.random.default_rng(n_clump)
+    xu, yu, zu = uniform_box(9, 100_000, L)
+    c = np.array([41.3, 57.9, 12.2])
+    clump = [c[a] + rng.uniform(-0.5, 0.5, n_clump) * (L / Ng) for a in range(3)]
+    x, y, z = (np.concatenate([u, v]).astype(np.float32).astype(np.float64) for u, v in zip((xu, yu, zu), clump))
+    V = L ** 3
+    g = fg.Grid(Ng, L, precision="f32", host_view="sync")
+    cat = fg.Catalog(x, y, z, V)
+    g.p2g(cat, [0.0, 0.0, 0.0])
+    o = oracle_lib.Oracle(Ng, L)
+    o.p2g(x, y, z, V, [0.0, 0.0, 0.0])
+    grid_close(g.real[..., :Ng], o.real[..., :Ng], 2e-5)
+    los, dK = (0.0, 0.0, 1.0), 2 * np.pi / L
+    got = g.power_f32(x, y, z, V, los, dK, Nmu=3)
+    want = oracle_lib.power_spectrum(Ng, L, x, y, z, los, dK, Nmu=3)
+    import parity
+    e = parity.errors(got, want, V / len(x), Ng, L)
+    assert parity.passes(e), e

@@ -155,3 +155,32 @@ def test_tma_i_pass_bit_identical(fg, tmp_path, Ng):
         assert r.returncode == 0, r.stderr[-2000:]
         outs[tma] = r.stdout.strip().splitlines()[-1]
     assert outs["1"] == outs["0"]
+
+
+def test_launch_shapes_measured_and_imported(fg, tmp_path):
+    """fft_init with a plan file also settles the tile paint's and the
+    binning's launch shapes: measured (or taken from this process's earlier
+    measurement) and written on a launch line of the file, imported from it by
+    the next grid; the spectra equal the built-in shapes' (paint bit for bit,
+    FP64 bin sums up to their order of addition)."""
+    path = tmp_path / "plan"
+    Ng = 128
+    g = fg.Grid(Ng, L_BOX, wisdom=str(path), precision="f32", host_view="lazy")
+    a = g.launch_shapes()
+    assert a["source"] in (fg.PLAN_MEASURED, fg.PLAN_CACHE)
+    assert a["paint_cta"] in (1, 2) and a["bin_cta"] in (1, 2, 3) and a["bin_fold"] in (0, 8, 32)
+    lines = [l for l in path.read_text().splitlines() if l.startswith("fftgal_gb300-launch 1 ")]
+    assert len(lines) == 1 and f" Ng={Ng} " in lines[0]
+    assert len(_entries(path)) == 1  # the FFT plan line is still there
+    h = fg.Grid(Ng, L_BOX, wisdom=str(path), precision="f32", host_view="lazy")
+    b = h.launch_shapes()
+    assert b["source"] == fg.PLAN_FILE
+    assert (b["paint_cta"], b["bin_cta"], b["bin_fold"]) == (a["paint_cta"], a["bin_cta"], a["bin_fold"])
+    rng = np.random.default_rng(8)
+    x, y, z = (rng.uniform(0, L_BOX, 300_000) for _ in range(3))
+    want = fg.Grid(Ng, L_BOX, precision="f32", host_view="lazy").power_f32(x, y, z, L_BOX ** 3, (0, 0, 1),
+                                                                          2 * np.pi / L_BOX)
+    got = h.power_f32(x, y, z, L_BOX ** 3, (0, 0, 1), 2 * np.pi / L_BOX)
+    np.testing.assert_array_equal(got["N"], want["N"])
+    ok = np.isfinite(want["P"])
+    np.testing.assert_allclose(got["P"][ok], want["P"][ok], rtol=1e-9, atol=1e-9 * np.abs(want["P"][ok]).max())
