@@ -638,6 +638,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}",
                        "fft_plan": {"source": ["built-in", "measured", "plan file", "process cache"][
                            grid.plan_info()["source"]], "tune": grid.plan_info()["tune"]},
+                       "launch_shapes": {k: v for k, v in grid.launch_shapes().items() if k != "ms"},
                        "particles_per_s": round(value * Np, 1),
                        "particles_per_s_e2e": round(e2e * Np, 1),
                        "stages_ms": stage_table,

@@ -448,6 +448,134 @@ fft2_cols_tma_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_const
             if (issued[s] > consumed[s]) mbar_wait(&full[s], (uint32_t)((issued[s] / kTmaStages) & 1));
 }
 
+// ---- the i pass of Ng = 1024 by even and odd rows (128-byte rows) ------------------------------
+// X[k] = E[k] + W_1024^k O[k], X[k + 512] = E[k] - W_1024^k O[k], with E and O
+// the 512-point transforms of the even and the odd rows of a column.  A tile
+// is 16 adjacent complex columns at one (grid, j) -- rows of 128 bytes -- and
+// is brought in as two half-tiles of 512 rows (64 KB each): the even rows,
+// then the odd rows, through a 3D tensor map (plane floats, row parity with
+// a stride of one plane, i / 2 with a stride of two planes; boxes of 32 floats
+// x 1 x 256).  Three 64 KB stages hold consecutive half-tiles; the CTA (512
+// threads, one per SM) transforms one half-tile while the next two are in
+// flight, keeping E in registers (16 values per thread) until O arrives.
+// A 512-point transform is 32 x 16: step 1 (256 threads, one per (column,
+// n2)) a 32-point FFT over n1 in place, twiddled by W_512^(n2 k1); step 2 (512
+// threads, one per (column, k1)) a 16-point FFT over n2.  Tiles start at
+// kc0 = 16 m + (j & 1) (16-byte aligned for every j); the column each j leaves
+// goes to fft2_cols_kernel.  Waits are bounded as in fft2_cols_tma_kernel.
+constexpr int kEoCols = 16;
+constexpr int kEoThreads = 512;
+constexpr int kEoHalfRows = 512;
+
+__global__ void __launch_bounds__(kEoThreads, 1)
+fft2_cols_tma_eo_kernel(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                        float2 *g0, float2 *g1, int ngrids, int Ng, int nh, int Ng_pad, long es,
+                        const float2 *__restrict__ W, int sign) {
+    constexpr int C = kEoCols, N1 = 32, N2 = 16, H = kEoHalfRows;
+    constexpr uint32_t kHalfBytes = H * C * sizeof(float2);
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    float2 *stages = reinterpret_cast<float2 *>(smem_raw);  // [kTmaStages][H][C]
+    __shared__ __align__(8) uint64_t full[kTmaStages];
+    __shared__ long issued[kTmaStages], consumed[kTmaStages];
+
+    const int ntj = (nh - 1) / C;  // tiles per (grid, j)
+    const long ntiles = (long)ngrids * Ng * ntj;
+    const long nloc = ntiles > (long)blockIdx.x ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const long nhalf = 2 * nloc;
+    const int t = threadIdx.x;
+
+    auto tile_of = [&](long l, int &g, int &j, int &kc0) {
+        const long q = blockIdx.x + (long)gridDim.x * l;
+        g = (int)(q / ((long)Ng * ntj));
+        const long r = q - (long)g * Ng * ntj;
+        j = (int)(r / ntj);
+        kc0 = C * (int)(r - (long)j * ntj) + (j & 1);
+    };
+    auto issue = [&](long h) {  // one thread: half-tile h (tile h / 2, rows of parity h & 1)
+        int g, j, kc0;
+        tile_of(h >> 1, g, j, kc0);
+        const int s = (int)(h % kTmaStages);
+        float2 *dst = stages + (size_t)s * H * C;
+        mbar_expect_tx(&full[s], kHalfBytes);
+        const CUtensorMap *tm = g ? &tm1 : &tm0;
+        const int x = j * Ng_pad + 2 * kc0, par = (int)(h & 1);
+#pragma unroll
+        for (int y = 0; y < H; y += kTmaBoxRows)
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(smem_addr(dst + (size_t)y * C)),
+                "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(par), "r"(y), "r"(smem_addr(&full[s]))
+                : "memory");
+        issued[s] = h;
+    };
+    if (t == 0) {
+        for (int s = 0; s < kTmaStages; ++s) {
+            mbar_init(&full[s], 1);
+            issued[s] = consumed[s] = -1;
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (long h = 0; h < kTmaStages && h < nhalf; ++h) issue(h);
+    }
+    __syncthreads();
+
+    float2 E[N2];  // this thread's even-row transform, kept until the odd rows arrive
+#pragma unroll
+    for (int q = 0; q < N2; ++q) E[q] = make_float2(0.f, 0.f);
+    const int c2 = t & (C - 1), k1 = t >> 4;  // step 2 and the output: (column, k1)
+    for (long h = 0; h < nhalf; ++h) {
+        const int s = (int)(h % kTmaStages);
+        const bool ok = mbar_wait(&full[s], (uint32_t)((h / kTmaStages) & 1));
+        if (!ok) atomicExch(&g_tma_err, 1);
+        if (__syncthreads_or(!ok)) break;  // the CTA leaves together
+        float2 *S = stages + (size_t)s * H * C;
+        if (t < C * N2) {  // step 1: x[N2 n1 + n2] -> Y[k1, n2] W_512^(n2 k1), in place
+            const int c = t & (C - 1), n2 = t >> 4;
+            float2 v[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; ++n1) v[n1] = S[(N2 * n1 + n2) * C + c];
+            reg_fft<N1>(v, sign);
+#pragma unroll
+            for (int q = 1; q < N1; ++q)
+                if (n2) v[q] = cmul(v[q], twid(W, 2 * n2 * q, sign));
+#pragma unroll
+            for (int q = 0; q < N1; ++q) S[(N2 * q + n2) * C + c] = v[q];
+        }
+        __syncthreads();
+        float2 u[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) u[n2] = S[(N2 * k1 + n2) * C + c2];
+        __syncthreads();
+        if (t == 0) {
+            consumed[s] = h;
+            if (h + kTmaStages < nhalf) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(h + kTmaStages);
+            }
+        }
+        reg_fft<N2>(u, sign);  // u[k2] = transform of this parity at k1 + 32 k2
+        if ((h & 1) == 0) {
+#pragma unroll
+            for (int q = 0; q < N2; ++q) E[q] = u[q];
+        } else {
+            int g, j, kc0;
+            tile_of(h >> 1, g, j, kc0);
+            float2 *base = (g ? g1 : g0) + (long)j * nh + kc0 + c2;
+#pragma unroll
+            for (int q = 0; q < N2; ++q) {
+                const int k = k1 + N1 * q;
+                const float2 wo = cmul(u[q], twid(W, k, sign));
+                base[(long)k * es] = cadd(E[q], wo);
+                base[(long)(k + N1 * N2) * es] = csub(E[q], wo);
+            }
+        }
+    }
+    __syncthreads();
+    if (t == 0)  // loads still in flight after a time-out land before the CTA exits
+        for (int s = 0; s < kTmaStages; ++s)
+            if (issued[s] > consumed[s]) mbar_wait(&full[s], (uint32_t)((issued[s] / kTmaStages) & 1));
+}
+
 // ---- host side ----------------------------------------------------------------------------
 
 static bool g_w32_ready = false;
@@ -593,6 +721,25 @@ static int plane_tensor_map(CUtensorMap *tm, void *grid, int Ng) {
     return OK;
 }
 
+// one FP32 grid as [Ng/2 plane pairs][2 row parities][Ng * Ng_pad floats],
+// boxes of 32 floats x 1 parity x 256 pairs (the even/odd i pass)
+static int parity_tensor_map(CUtensorMap *tm, void *grid, int Ng) {
+    EncodeTiledFn enc;
+    FG_TRY(tensor_map_encoder(&enc));
+    const cuuint64_t Ng_pad = 2 * (cuuint64_t)(Ng / 2 + 1), plane = (cuuint64_t)Ng * Ng_pad;
+    const cuuint64_t dims[3] = {plane, 2, (cuuint64_t)Ng / 2};
+    const cuuint64_t strides[2] = {plane * sizeof(float), 2 * plane * sizeof(float)};
+    const cuuint32_t box[3] = {2 * kEoCols, 1, (cuuint32_t)kTmaBoxRows};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    if (reinterpret_cast<uintptr_t>(grid) % 16 || strides[0] % 16)
+        return set_error(ERR_UNSUPPORTED, "TMA i pass: grid address or plane stride not 16-byte aligned");
+    const CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, grid, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return OK;
+}
+
 bool fft2_tma_supported(int Ng, int prec) {
     // off by default: with 64-byte rows at the plane stride the TMA pass
     // measured 7.8 ms against 4.7 ms for fft2_cols_kernel (16 columns, 128-byte
@@ -616,10 +763,15 @@ int fft2_cols_tma(int Ng, const void *W, void *g0, void *g1, int ngrids, int sig
     const size_t smem = (size_t)kTmaStages * Ng * kTmaCols * sizeof(float2);
     const long ntiles = (long)ngrids * Ng * ((nh - 1) / kTmaCols);
     const unsigned nb = (unsigned)(ntiles < num_sms() ? ntiles : num_sms());
-    if (Ng == 1024) {
-        FG_CUDA(cudaFuncSetAttribute(fft2_cols_tma_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fft2_cols_tma_kernel<32><<<nb, kTmaThreads, smem, s>>>(tm[0], tm[1], (float2 *)g0, (float2 *)b, ngrids, Ng,
-                                                               nh, Ng_pad, es, (const float2 *)W, sign);
+    if (Ng == 1024) {  // even and odd rows: 16 columns, 128-byte rows
+        FG_TRY(parity_tensor_map(&tm[0], g0, Ng));
+        FG_TRY(parity_tensor_map(&tm[1], b, Ng));
+        const size_t esmem = (size_t)kTmaStages * kEoHalfRows * kEoCols * sizeof(float2);
+        const long etiles = (long)ngrids * Ng * ((nh - 1) / kEoCols);
+        const unsigned enb = (unsigned)(etiles < num_sms() ? etiles : num_sms());
+        FG_CUDA(cudaFuncSetAttribute(fft2_cols_tma_eo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
+        fft2_cols_tma_eo_kernel<<<enb, kEoThreads, esmem, s>>>(tm[0], tm[1], (float2 *)g0, (float2 *)b, ngrids, Ng,
+                                                                nh, Ng_pad, es, (const float2 *)W, sign);
     } else {
         FG_CUDA(cudaFuncSetAttribute(fft2_cols_tma_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         fft2_cols_tma_kernel<16><<<nb, kTmaThreads, smem, s>>>(tm[0], tm[1], (float2 *)g0, (float2 *)b, ngrids, Ng,

@@ -121,7 +121,8 @@ Ng = int(sys.argv[2])
 Ngp = 2 * (Ng // 2 + 1)
 g = fg.Grid(Ng, float(Ng), precision="f32", host_view="lazy")
 gen = torch.Generator(device="cuda").manual_seed(Ng)
-x = torch.randn((Ng, Ng, Ngp), generator=gen, device="cuda", dtype=torch.float32)
+x0 = torch.randn((Ng, Ng, Ngp), generator=gen, device="cuda", dtype=torch.float32)
+x = x0.clone()
 w = (torch.arange(x.numel(), device="cuda", dtype=torch.int64) % 1000003) + 1
 def digest(t):
     b = t.view(torch.int32).reshape(-1).to(torch.int64)
@@ -130,19 +131,26 @@ g.copy_from(x.data_ptr())
 g.x2k(0)
 g.copy_to(x.data_ptr())
 k = digest(x)
+got = torch.view_as_complex(x.view(Ng, Ng, Ngp // 2, 2)).to(torch.complex128)
+ref = torch.fft.rfftn(x0[..., :Ng].double())
+fwd = float(torch.linalg.vector_norm(got - ref) / torch.linalg.vector_norm(ref))
+del got, ref
 g.k2x(0)
 g.copy_to(x.data_ptr())
-print(k + digest(x))
+back = float(torch.linalg.vector_norm((x - x0)[..., :Ng].double()) / torch.linalg.vector_norm(x0[..., :Ng].double()))
+print(k + digest(x), fwd, back)
 """
 
 
 @pytest.mark.parametrize("Ng", [512, 1024])
-def test_tma_i_pass_bit_identical(fg, tmp_path, Ng):
-    """The TMA-staged i pass (Ng = 512 and 1024, selected by FFTGAL_TMA=1)
-    transforms every column with the same decomposition and twiddles as the
-    register-staged column kernel: forward and backward grids are
-    bit-identical to a run without it (compared through integer checksums of
-    their bits)."""
+def test_tma_i_pass(fg, tmp_path, Ng):
+    """The TMA-staged i pass (FFTGAL_TMA=1): forward and backward transforms
+    within the FP32 bounds of the cuFFT cross-check (relative L2 error <= 1e-6
+    against torch.fft in FP64, and of the round trip); at Ng = 512 (columns
+    split 32 x 16 like the register-staged kernel) the grids are bit-identical
+    to a run without it, at Ng = 1024 (even and odd rows, two 512-point
+    transforms) the decomposition differs, so only the bounds apply."""
+    import ast
     import os
     import subprocess
     import sys
@@ -151,10 +159,15 @@ def test_tma_i_pass_bit_identical(fg, tmp_path, Ng):
     for tma in ("1", "0"):
         env = dict(os.environ, FFTGAL_TMA=tma, FFTGAL_QUIET="1")
         r = subprocess.run([sys.executable, "-c", _TMA_CHILD, root, str(Ng)], env=env,
-                           capture_output=True, text=True, timeout=600)
+                           capture_output=True, text=True, timeout=900)
         assert r.returncode == 0, r.stderr[-2000:]
-        outs[tma] = r.stdout.strip().splitlines()[-1]
-    assert outs["1"] == outs["0"]
+        line = r.stdout.strip().splitlines()[-1]
+        head, fwd, back = line.rsplit(" ", 2)
+        outs[tma] = (ast.literal_eval(head), float(fwd), float(back))
+    for tma in ("1", "0"):
+        assert outs[tma][1] <= 1e-6 and outs[tma][2] <= 1e-6, (tma, outs[tma])
+    if Ng == 512:
+        assert outs["1"][0] == outs["0"][0]
 
 
 def test_launch_shapes_measured_and_imported(fg, tmp_path):
