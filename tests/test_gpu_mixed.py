@@ -1,9 +1,10 @@
 """fftgal_power_mixed_f32: catalogs of mixed grid sizes (powers of two and
 not), fold factors (box L / fold, src/app/P.c:35-36), bin widths and uneven
 particle counts in one call.  Every catalog's tables equal fftgal_power_f32's
-on a grid of its own (the binning's FP64 sums are added in a different order:
-1e-10 of |P_0| + Pshot), a subset matches the FP64 oracle under the parity
-criterion, and a second call reuses the kept grids."""
+on a grid of its own up to the order in which the binning adds its sums (the
+FP32 shared-memory run sums and the FP64 global sums are atomic: 1e-6 of
+|P_0| + Pshot; mode counts exact), a subset matches the FP64 oracle under the
+parity criterion, and a second call reuses the kept grids."""
 import numpy as np
 import pytest
 
@@ -57,7 +58,7 @@ def test_mixed_matches_single_calls(fg, oracle_lib):
     for c, (x, y, z) in enumerate(cats):
         g = fg.Grid(Ng[c], L[c], precision="f32", host_view="lazy")
         want = g.power_f32(x, y, z, V, los, dK[c], Nmu=Nmu)
-        _close(res[c], want, V / len(x), 1e-10)
+        _close(res[c], want, V / len(x), 1e-6)
     for c in (0, 1, 6):  # a power of two and not, folds 1, 2 and 4
         x, y, z = (a.astype(np.float64) for a in cats[c])
         want = oracle_lib.power_spectrum(Ng[c], L[c], x, y, z, los, dK[c], Nmu=Nmu, V=V)
@@ -65,7 +66,7 @@ def test_mixed_matches_single_calls(fg, oracle_lib):
         assert parity.passes(e), (c, e)
     again = fg.power_mixed_f32(cats[::-1], V, Ng[::-1], L[::-1], los, dK[::-1], Nmu=Nmu)
     for c in range(len(cats)):
-        _close(again[len(cats) - 1 - c], res[c], V / len(cats[c][0]), 1e-10)
+        _close(again[len(cats) - 1 - c], res[c], V / len(cats[c][0]), 1e-6)
     fg.power_mixed_release()
 
 

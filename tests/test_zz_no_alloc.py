@@ -98,7 +98,8 @@ def test_noalloc_allocates_nothing(fg):
     for nmu in (3, 10, 16, 3):
         got = fg.power_bins_noalloc(*args, Nmu=nmu)
         assert torch.cuda.mem_get_info()[0] == free0
-    np.testing.assert_array_equal(got["P"], first["P"])
+    # the same tables again, up to the order of the atomic additions
+    _close(got, first, L ** 3 / n)
 
 
 def test_noalloc_limits(fg):
@@ -139,7 +140,9 @@ def test_noalloc_ng2048_geometry(fg):
     assert int(got["N"].sum()) == Ng ** 3 - 1
     np.testing.assert_array_equal(got["Nmu"].sum(axis=1), got["N"])
     Pshot = V / Np
-    np.testing.assert_allclose(got["P"][:, 0], -Pshot, rtol=1e-5)
+    full = got["N"] > 0  # bin 0 holds no mode at dK = 2 pi / L: NaN, as the reference prints it
+    assert not full[0] and full[1:].all() and np.isnan(got["P"][0]).all()
+    np.testing.assert_allclose(got["P"][full, 0], -Pshot, rtol=1e-5)
     filled = got["Nmu"] > 0
     np.testing.assert_allclose(got["Pmu"][filled], -Pshot, rtol=1e-5)
-    assert np.all(np.isfinite(got["P"]))
+    assert np.all(np.isfinite(got["P"][full]))
