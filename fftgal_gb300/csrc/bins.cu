@@ -325,8 +325,50 @@ struct SlabFinish {
     float scale = 0.f;           // H^3 / 2
 };
 
+// The slab blocks cover k < kmain.  When the half spectrum's last k block
+// would hold only one or two columns (nh = Ng/2 + 1: the Nyquist column of
+// every even Ng that is a multiple of 32), those columns are binned mode by
+// mode after the blocks instead, by all threads of the grid, rather than as
+// 32-column blocks with one or two columns used (6 % of the lane slots at
+// Ng = 1024).
+__host__ __device__ __forceinline__ int slab_kmain(int nh) {
+    const int r = nh % kSlabK;
+    return (nh > kSlabK && r > 0 && r <= 2) ? nh - r : nh;
+}
+
+// |delta|^2 Vinv - Pshot of element e.  MODE 2 to 5 finish it first, with the
+// phase pf * phr (MODE 2 and 5) and the window inverse wf * wr; MODE 2 and 3
+// store the finished value.
 template <int MODE>
-__global__ void __launch_bounds__(kSlabThreads, 3)
+__device__ __forceinline__ float mode_power(const SlabFinish &fin, const float2 *__restrict__ f, long e, float2 pf,
+                                           float2 phr, float wf, float wr, float Vinv, float Pshot) {
+    if (MODE == 2 || MODE == 5) {
+        const float2 p = cmul(pf, phr);
+        const float wk = wf * wr;
+        const float2 bv = fin.B[e], av = fin.A[e];
+        const float2 dv = cmul(bv, p);
+        const float2 v = make_float2((dv.x + av.x) * wk, (dv.y + av.y) * wk);
+        if (MODE == 2) fin.A[e] = v;
+        return (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+    } else if (MODE == 3 || MODE == 4) {
+        const float wk = wf * wr;
+        const float2 av = fin.A[e];
+        const float2 v = make_float2(av.x * wk, av.y * wk);
+        if (MODE == 3) fin.A[e] = v;
+        return (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+    } else if (MODE == 1) {
+        const float2 v = f[e];
+        return (v.x * v.x + v.y * v.y) * Vinv - Pshot;
+    } else {
+        return f[e].x;
+    }
+}
+
+// MINB: CTAs per SM the registers are budgeted for (3: 40 registers with a
+// few spills, 2: no spills), chosen by the CTAs per SM that the launch's
+// shared memory allows and the tuned launch shape
+template <int MODE, int MINB>
+__global__ void __launch_bounds__(kSlabThreads, MINB)
 bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, float Vinv, float Pshot,
                       const uint32_t *__restrict__ thr_g, double *__restrict__ gacc, const DevScalars *__restrict__ ds,
                       int fold) {
@@ -344,8 +386,8 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
     for (int e = tid; e < NK * NQ; e += blockDim.x) acc32[e] = 0.f;
     for (int e = tid; e < NK + 2; e += blockDim.x) thr[e] = thr_g[e];
     __syncthreads();
-    const int Ng = d.Ng, nh = d.nh;
-    const int nbi = (Ng + kSlabI - 1) / kSlabI, nbj = (Ng + kSlabJ - 1) / kSlabJ, nbk = (nh + kSlabK - 1) / kSlabK;
+    const int Ng = d.Ng, nh = d.nh, kmain = slab_kmain(nh);
+    const int nbi = (Ng + kSlabI - 1) / kSlabI, nbj = (Ng + kSlabJ - 1) / kSlabJ, nbk = (kmain + kSlabK - 1) / kSlabK;
     const int nblk = nbi * nbj * nbk;
     int since_fold = 0;
     for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
@@ -364,7 +406,7 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
         if (fixed < Ng) {
             float2 pfk = make_float2(0.f, 0.f);
             float wfk = 0.f;
-            if (MODE >= 2 && k < nh) {
+            if (MODE >= 2 && k < kmain) {
                 if (MODE == 2 || MODE == 5) pfk = cmul(fin.ph[(rows_i ? Ng : 0) + fixed], fin.ph[2 * Ng + k]);
                 wfk = fin.w[fixed] * fin.w[k] * fin.scale;
             }
@@ -372,28 +414,11 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
             for (int r = 0; r < kSlabJ; ++r) {
                 const int rr = r0 + r;
                 float pv = 0.f;
-                if (rr < Ng && k < nh) {
+                if (rr < Ng && k < kmain) {
                     const long e = (rows_i ? ((long)rr * Ng + fixed) : ((long)fixed * Ng + rr)) * nh + k;
-                    if (MODE == 2 || MODE == 5) {
-                        const float2 p = cmul(pfk, fin.ph[(rows_i ? 0 : Ng) + rr]);
-                        const float wk = wfk * fin.w[rr];
-                        const float2 bv = fin.B[e], av = fin.A[e];
-                        const float2 dv = cmul(bv, p);
-                        const float2 v = make_float2((dv.x + av.x) * wk, (dv.y + av.y) * wk);
-                        if (MODE == 2) fin.A[e] = v;
-                        pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
-                    } else if (MODE == 3 || MODE == 4) {
-                        const float wk = wfk * fin.w[rr];
-                        const float2 av = fin.A[e];
-                        const float2 v = make_float2(av.x * wk, av.y * wk);
-                        if (MODE == 3) fin.A[e] = v;
-                        pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
-                    } else if (MODE == 1) {
-                        const float2 v = f[e];
-                        pv = (v.x * v.x + v.y * v.y) * Vinv - Pshot;
-                    } else {
-                        pv = f[e].x;
-                    }
+                    const float2 phr = (MODE == 2 || MODE == 5) ? fin.ph[(rows_i ? 0 : Ng) + rr] : make_float2(0.f, 0.f);
+                    const float wr = MODE >= 2 ? fin.w[rr] : 0.f;
+                    pv = mode_power<MODE>(fin, f, e, pfk, phr, wfk, wr, Vinv, Pshot);
                 }
                 slab[r * kSlabRow + lane] = pv;
             }
@@ -406,7 +431,7 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
             BinRun run;
             for (int t = 0; t < 16; ++t, r += dr, c += dc) {
                 const int rr = r0 + r, kc = k0 + c;
-                if (rr >= Ng || kc >= nh) continue;
+                if (rr >= Ng || kc >= kmain) continue;
                 const int i = rows_i ? rr : fixed, j = rows_i ? fixed : rr;
                 if ((i | j | kc) == 0) continue;  // the k = 0 mode (src/power.c:52-54)
                 run.add(d, thr, acc32, kval(i, Ng), kval(j, Ng), kval(kc, Ng), kc, slab[r * kSlabRow + c]);
@@ -419,6 +444,33 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
             __syncthreads();
             bin_fold(acc32, gacc, NK, NQ);
             __syncthreads();
+        }
+    }
+    // the columns k >= kmain, one mode per thread (consecutive threads take
+    // consecutive j; the finish takes the phase and window products in the
+    // order of the blocks that run along i)
+    if (kmain < nh) {
+        const int ncol = nh - kmain;
+        const long nplane = (long)ncol * Ng * Ng;
+        for (long m = (long)blockIdx.x * blockDim.x + tid; m < nplane; m += (long)gridDim.x * blockDim.x) {
+            const int kc = kmain + (int)(m % ncol);
+            const long ij = m / ncol;
+            const int j = (int)(ij % Ng), i = (int)(ij / Ng);
+            const long e = ((long)i * Ng + j) * nh + kc;
+            float2 pf = make_float2(0.f, 0.f), phr = make_float2(0.f, 0.f);
+            float wf = 0.f, wr = 0.f;
+            if (MODE == 2 || MODE == 5) {
+                pf = cmul(fin.ph[Ng + j], fin.ph[2 * Ng + kc]);
+                phr = fin.ph[i];
+            }
+            if (MODE >= 2) {
+                wf = fin.w[j] * fin.w[kc] * fin.scale;
+                wr = fin.w[i];
+            }
+            const float pv = mode_power<MODE>(fin, f, e, pf, phr, wf, wr, Vinv, Pshot);
+            BinRun run;
+            run.add(d, thr, acc32, kval(i, Ng), kval(j, Ng), kval(kc, Ng), kc, pv);
+            run.finish(d, acc32);
         }
     }
     __syncthreads();
@@ -479,7 +531,7 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
         int per_sm = (int)((224 * 1024) / (smem + 1024));
         per_sm = per_sm < 1 ? 1 : (per_sm > 3 ? 3 : per_sm);
         if (g->cta_per_sm > 0 && g->cta_per_sm < per_sm) per_sm = g->cta_per_sm;  // tuned shape
-        const long nblk = ceil_div(s.Ng, kSlabI) * ceil_div(s.Ng, kSlabJ) * ceil_div(s.Ng / 2 + 1, kSlabK);
+        const long nblk = ceil_div(s.Ng, kSlabI) * ceil_div(s.Ng, kSlabJ) * ceil_div(slab_kmain(s.Ng / 2 + 1), kSlabK);
         long nb = (long)num_sms() * per_sm;
         if (nb > nblk) nb = nblk;
         SlabFinish sf;
@@ -491,12 +543,19 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
             sf.scale = (float)fin->scale;
         }
         const float2 *fv = static_cast<const float2 *>(mode >= 2 ? fin->A : f);
-#define FG_SLAB_LAUNCH(M)                                                                                   \
+#define FG_SLAB_LAUNCH2(M, B)                                                                                \
     do {                                                                                                    \
-        FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+        FG_CUDA(cudaFuncSetAttribute(bin_power_slab_kernel<M, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)smem));                                                           \
-        bin_power_slab_kernel<M><<<(unsigned)nb, kSlabThreads, smem, st>>>(d, fv, sf, (float)Vinv, (float)Pshot, \
-                                                                         g->d_thr, g->d_acc, ds, g->fold > 0 ? g->fold : fold_blocks()); \
+        bin_power_slab_kernel<M, B><<<(unsigned)nb, kSlabThreads, smem, st>>>(                              \
+            d, fv, sf, (float)Vinv, (float)Pshot, g->d_thr, g->d_acc, ds, g->fold > 0 ? g->fold : fold_blocks()); \
+    } while (0)
+#define FG_SLAB_LAUNCH(M)             \
+    do {                              \
+        if (per_sm >= 3)              \
+            FG_SLAB_LAUNCH2(M, 3);    \
+        else                          \
+            FG_SLAB_LAUNCH2(M, 2);    \
     } while (0)
         if (mode == 0)
             FG_SLAB_LAUNCH(0);
@@ -510,6 +569,7 @@ static int bin_launch(BinGeometry *g, const void *f, int prec, int mode, double 
             FG_SLAB_LAUNCH(4);
         else
             FG_SLAB_LAUNCH(5);
+#undef FG_SLAB_LAUNCH2
 #undef FG_SLAB_LAUNCH
     } else {
         const int Ng_pad = 2 * (s.Ng / 2 + 1);

@@ -239,6 +239,30 @@ def test_mode_counts_exact(fg, oracle_lib, small, Ng, Nmu):
             np.testing.assert_allclose(r["Kmu"], Km, rtol=1e-12)
 
 
+@pytest.mark.parametrize("Ng", [64, 65, 66, 48])
+def test_last_k_columns(fg, oracle_lib, Ng):
+    """The finish + binning kernel bins the last one or two k columns mode by
+    mode after its 16 x 16 x 32 blocks when they would fill a block of their
+    own (Ng = 64: the Nyquist column; 65: the last column of an odd grid; 66:
+    two columns) and not otherwise (48).  The fused call under the lazy view
+    (finished field binned, not stored) and under the sync view (stored)
+    against the FP64 oracle: the tables under the parity criterion, and the
+    stored k-space grid within 1e-5 of its largest value."""
+    import parity
+    L, n = 200.0, 100_000
+    x, y, z = (np.asarray(a, dtype=np.float32).astype(np.float64) for a in uniform_box(17, n, L))
+    V, los, dK = L ** 3, (0.3, 0.5, 1.0), 2 * np.pi / L
+    want = oracle_lib.power_spectrum(Ng, L, x, y, z, los, dK, Nmu=4)
+    for view in ("lazy", "sync"):
+        g = fg.Grid(Ng, L, precision="f32", host_view=view)
+        got = g.power_f32(x, y, z, V, los, dK, Nmu=4)
+        e = parity.errors(got, want, V / n, Ng, L)
+        assert parity.passes(e), (view, e)
+    o = oracle_lib.Oracle(Ng, L)
+    o.p2k(x, y, z, V)
+    grid_close(np.array(g.cplx), np.array(o.cplx), 1e-5)
+
+
 def test_fp32_paint_is_bit_reproducible(fg):
     x, y, z = uniform_box(11, 200_000, 500.0)
     g = fg.Grid(64, 500.0, precision="f32", host_view="lazy")
