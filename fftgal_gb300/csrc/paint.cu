@@ -30,8 +30,13 @@
 // per-tile scale 2^-s, s the largest value for which no cell can exceed 2^32 (a
 // particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
 // total bounds every cell, and only where that bound leaves fewer than 21
-// fraction bits does a first pass count particles per 4^3-cell block.  Integer sums are order
-// independent, so the painted grid is bit-reproducible run to run.
+// fraction bits does a first pass count particles per 4^3-cell block.  A tile
+// whose bound still leaves fewer than 20 bits (a dense clump: more than about
+// 14000 particles near one cell) paints one grid at a time into 64-bit sums
+// with 22 fraction bits over the same shared memory, since at 12-16 bits the
+// many tiny products at a stencil's edge round to zero and bias the edge cells
+// low.  Integer sums are order independent, so the painted grid is
+// bit-reproducible run to run.
 // FP64 grids (paint_tile_f64_kernel) reproduce the reference's FP64 weight
 // arithmetic op for op and accumulate in FP64, one thread per particle.
 #include "internal.h"
@@ -45,7 +50,10 @@ namespace fg {
 
 constexpr int kTileExt[3] = {16, 16, 32};    // i, j, k
 constexpr int kMaxPaintGrids = 2;
-constexpr int kMinFixBits = 8;                 // below this: FP32 accumulation
+// dense tiles (fewer 32-bit fraction bits than kWideBelow): 64-bit sums with
+// kWideBits fraction bits, one grid per pass
+constexpr int kWideBelow = 20;
+constexpr int kWideBits = 22;
 // FP32 shared layout: cell (li, lj, lk) of grid g at g*kGS + li*kSI + lj*kSJ +
 // kPadK + lk.  kSI = 8 and kSJ = 6 (mod 32) put the 16 rows (li+a, lj+b), a, b
 // < 4, of one stencil in 16 distinct banks of one parity, and the odd kGS gives
@@ -529,14 +537,16 @@ __device__ __forceinline__ uint32_t pack_local(int b, int Ng, int t0, int te, ui
 // interleave so that lanes reading both fall in different banks
 __device__ __forceinline__ int stage_slot(int p, int g) { return 2 * p + g; }
 
-template <bool FIXED>
-__device__ __forceinline__ void dep_one(uint32_t *cell, float w, float wz) {
-    if (FIXED) {
-        const float M = 12582912.0f;  // 1.5 * 2^23: FMA onto it rounds w * wz to an integer
-        atomicAdd(cell, __float_as_uint(fmaf(w, wz, M)) - 0x4B400000u);
-    } else {
-        atomicAdd(reinterpret_cast<float *>(cell), w * wz);
-    }
+// add round(w * wz) to the cell at offset `off`: 32-bit sums, or 64-bit sums
+// (WIDE, offsets counted in 64-bit cells); w * wz < 2^22
+template <bool WIDE>
+__device__ __forceinline__ void dep_one(uint32_t *acc, int off, float w, float wz) {
+    const float M = 12582912.0f;  // 1.5 * 2^23: FMA onto it rounds w * wz to an integer
+    const uint32_t q = __float_as_uint(fmaf(w, wz, M)) - 0x4B400000u;
+    if (WIDE)
+        atomicAdd(reinterpret_cast<unsigned long long *>(acc) + off, (unsigned long long)q);
+    else
+        atomicAdd(acc + off, q);
 }
 
 // One particle of grid g for lane (a, b).
@@ -548,7 +558,7 @@ __device__ __forceinline__ void dep_one(uint32_t *cell, float w, float wz) {
 // Otherwise loc.x / loc.y hold the 4 local i / j indices as bytes (kOut outside
 // the tile) and loc.z the 4 padded k cells as bytes, in step order.
 // The k weights are stored in step order.
-template <bool FIXED, bool FAST>
+template <bool WIDE, bool FAST>
 __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, int slot, int g, int a, int b,
                                             int lane_off) {
     const uint4 loc = sb.loc[slot];
@@ -557,43 +567,43 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
     const float4 wz = sb.w[2][slot];
     if (FAST) {
         if (!((loc.z >> (4 * a + b)) & 1u)) return;  // a stencil row outside the tile
-        uint32_t *p0 = acc + (int)loc.x + lane_off;
-        uint32_t *p1 = acc + (int)loc.y + lane_off;
-        dep_one<FIXED>(p0, w, wz.x);
-        dep_one<FIXED>(p1, w, wz.y);
-        dep_one<FIXED>(p0 + 2, w, wz.z);
-        dep_one<FIXED>(p1 + 2, w, wz.w);
+        const int o0 = (int)loc.x + lane_off, o1 = (int)loc.y + lane_off;
+        dep_one<WIDE>(acc, o0, w, wz.x);
+        dep_one<WIDE>(acc, o1, w, wz.y);
+        dep_one<WIDE>(acc, o0 + 2, w, wz.z);
+        dep_one<WIDE>(acc, o1 + 2, w, wz.w);
     } else {
         const uint32_t li = (loc.x >> (8 * a)) & 255u;
         const uint32_t lj = (loc.y >> (8 * b)) & 255u;
         if ((li | lj) >= 16u) return;
-        uint32_t *row = acc + g * kGS + li * kSI + lj * kSJ;
-        dep_one<FIXED>(row + (loc.z & 255u), w, wz.x);
-        dep_one<FIXED>(row + ((loc.z >> 8) & 255u), w, wz.y);
-        dep_one<FIXED>(row + ((loc.z >> 16) & 255u), w, wz.z);
-        dep_one<FIXED>(row + (loc.z >> 24), w, wz.w);
+        const int row = g * kGS + (int)(li * kSI + lj * kSJ);
+        dep_one<WIDE>(acc, row + (int)(loc.z & 255u), w, wz.x);
+        dep_one<WIDE>(acc, row + (int)((loc.z >> 8) & 255u), w, wz.y);
+        dep_one<WIDE>(acc, row + (int)((loc.z >> 16) & 255u), w, wz.z);
+        dep_one<WIDE>(acc, row + (int)(loc.z >> 24), w, wz.w);
     }
 }
 
-template <bool FIXED, bool FAST>
+template <bool WIDE, bool FAST>
 __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, int np, int ngr, int lane) {
     const int h = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
     const int lane_off = a * kSI + b * kSJ;
     if (ngr > 1) {
 #pragma unroll 4
-        for (int p = 0; p < np; ++p) deposit_one<FIXED, FAST>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
+        for (int p = 0; p < np; ++p) deposit_one<WIDE, FAST>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
     } else {
         // one grid: 32 particles staged in slots 0..31, the half warps
         // deposit alternate ones
 #pragma unroll 2
-        for (int p = h; p < np; p += 2) deposit_one<FIXED, FAST>(acc, sb, p, 0, a, b, lane_off);
+        for (int p = h; p < np; p += 2) deposit_one<WIDE, FAST>(acc, sb, p, 0, a, b, lane_off);
     }
 }
 
 // largest fixed-point exponent s for which `n` contributors to one cell cannot
 // overflow its 32-bit sum: each adds round(w 2^s) <= 8/27 2^s + 1/2 (the
 // largest PCS weight product is (2/3)^3), so n (16 2^s + 27) < 54 2^32 is
-// required.  Exact integer arithmetic; a negative result selects FP32 sums.
+// required.  Exact integer arithmetic; a result below kWideBelow selects the
+// 64-bit sums.
 __device__ __forceinline__ int fix_bits_for(uint32_t n) {
     if (n == 0) return kMaxFixBits;
     const unsigned long long x = (54ull << 32) / n;
@@ -748,147 +758,185 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             __syncthreads();
             fixbits = fixbits_s;
         }
-        const bool fixed = fixbits >= kMinFixBits;
-        const float fscale = ldexpf(1.0f, fixed ? fixbits : 0);
-
-        // pass B: each warp stages 16 particles for both grids (lanes 0..15
-        // grid 0, 16..31 grid 1), or 32 particles for one grid, then deposits
-        // them; the records of the warp's next batch are loaded before the
-        // deposit so their latency hides behind it
-        StageBuf &sb = stage[warp];
+        // a dense tile paints one grid per pass into 64-bit sums; otherwise
+        // one pass paints every grid into 32-bit sums
+        const bool wide = fixbits < kWideBelow;
+        const int npass = wide ? ngr : 1;
+        const float fscale = ldexpf(1.0f, wide ? kWideBits : fixbits);
+        const int ngs = wide ? 1 : ngr;  // grids staged per round
+        if (wide) {
+            // the 32-bit tiles leave sums in the row padding: clear all of it
+            __syncthreads();
+            for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
+                reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+        }
         const bool fast = !(cyc[0] || cyc[1] || cyc[2]);
-        const int parts = ngr > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
-        const int gs = ngr > 1 ? lane / kStageParts : 0;
-        const uint32_t bstride = (uint32_t)nwarp * parts;
-        uint32_t base = (uint32_t)warp * parts;
-        uint4 rec = make_uint4(0, 0, 0, 0);
-        {
-            const uint32_t q = base + (lane & (parts - 1));
-            if (q < total) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
-        }
-        for (; base < total; base += bstride) {
-            const uint32_t q = base + (lane & (parts - 1));
-            if (q < total) {
-                const uint32_t rw[3] = {rec.x, rec.y, rec.z};
-                const float inv = ldexpf(1.0f, -fb);
-                const int slot = ngr > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
-                int bgv[3], lv[3];
-                uint32_t par = 0;
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const int b0 = (int)(rw[a] >> fb);
-                    int bg;
-                    uint32_t dgq;
-                    cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
-                    float w[4];
-                    pcs_weights((float)dgq * inv, w);
-                    float4 wv = make_float4(w[0], w[1], w[2], w[3]);
-                    if (a == 2) {
-                        wv = make_float4(wv.x * fscale, wv.y * fscale, wv.z * fscale, wv.w * fscale);
-                        par = (uint32_t)(bg - b0) & 1u;
-                        if (par) wv = make_float4(wv.y, wv.x, wv.w, wv.z);  // k cells in the order s ^ 1
-                    }
-                    sb.w[a][slot] = wv;
-                    // local index of the first stencil cell (periodic images
-                    // folded to the nearest copy of the tile)
-                    int l = bg - 1 - ts.t0[a];
-                    l -= l > Ng / 2 ? Ng : 0;
-                    l += l < -Ng / 2 ? Ng : 0;
-                    bgv[a] = bg;
-                    lv[a] = l;
-                }
-                const bool kmiss = !cyc[2] && (lv[2] < -3 || lv[2] >= ts.te[2]);  // stencil misses the tile
-                uint4 loc;
-                if (fast) {
-                    const uint32_t mi = (unsigned)(lv[0] + 4) < 40u ? masktab[0][lv[0] + 4] : 0u;
-                    const uint32_t mj = (unsigned)(lv[1] + 4) < 40u ? masktab[1][lv[1] + 4] : 0u;
-                    const int b0 = gs * kGS + lv[0] * kSI + lv[1] * kSJ + lv[2] + kPadK + (int)par;
-                    loc = make_uint4((uint32_t)b0, (uint32_t)(b0 + 1 - 2 * (int)par), kmiss ? 0u : mi * mj, 0u);
-                } else {
-                    uint32_t li, lj, lk;
-                    li = cyc[0] ? pack_local(bgv[0], Ng, ts.t0[0], ts.te[0], kOut)
-                                : ((unsigned)(lv[0] + 4) < 40u ? loctab[0][lv[0] + 4] : 0xFFFFFFFFu);
-                    lj = cyc[1] ? pack_local(bgv[1], Ng, ts.t0[1], ts.te[1], kOut)
-                                : ((unsigned)(lv[1] + 4) < 40u ? loctab[1][lv[1] + 4] : 0xFFFFFFFFu);
-                    if (cyc[2])
-                        lk = pack_local(bgv[2], Ng, ts.t0[2], ts.te[2], 0u) + 0x01010101u * kPadK;
-                    else
-                        lk = (uint32_t)(kmiss ? 0 : lv[2] + kPadK) * 0x01010101u + 0x03020100u;
-                    if (par) lk = ((lk & 0x00FF00FFu) << 8) | ((lk >> 8) & 0x00FF00FFu);
-                    loc = make_uint4(kmiss ? 0xFFFFFFFFu : li, lj, lk, 0u);
-                }
-                sb.loc[slot] = loc;
-            }
-            __syncwarp();
-            {
-                const uint32_t qn = base + bstride + (lane & (parts - 1));
-                if (qn < total) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
-            }
-            const int np = min((uint32_t)parts, total - base);
-            if (fast) {
-                if (fixed)
-                    deposit_all<true, true>(acc, sb, np, ngr, lane);
-                else
-                    deposit_all<false, true>(acc, sb, np, ngr, lane);
-            } else {
-                if (fixed)
-                    deposit_all<true, false>(acc, sb, np, ngr, lane);
-                else
-                    deposit_all<false, false>(acc, sb, np, ngr, lane);
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-
-        // the next tile's segments, loaded now and published after the write-out
         const unsigned next = tile + gridDim.x;
         uint32_t nb_begin = 0, nb_cnt = 0;
         int nb_comb = 0;
-        if (next < ntiles) nb_comb = tile_segment(pp, off, next, tid, nb_begin, nb_cnt);
+        for (int pass = 0; pass < npass; ++pass) {
+            // pass B: each warp stages 16 particles for both grids (lanes 0..15
+            // grid 0, 16..31 grid 1), or 32 particles for one grid, then deposits
+            // them; the records of the warp's next batch are loaded before the
+            // deposit so their latency hides behind it
+            StageBuf &sb = stage[warp];
+            const int parts = ngs > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
+            const int gs = ngs > 1 ? lane / kStageParts : pass;           // the grid this lane stages
+            const int gofs = wide ? 0 : gs * kGS;                         // and its accumulator
+            const uint32_t bstride = (uint32_t)nwarp * parts;
+            uint32_t base = (uint32_t)warp * parts;
+            uint4 rec = make_uint4(0, 0, 0, 0);
+            {
+                const uint32_t q = base + (lane & (parts - 1));
+                if (q < total) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+            }
+            for (; base < total; base += bstride) {
+                const uint32_t q = base + (lane & (parts - 1));
+                if (q < total) {
+                    const uint32_t rw[3] = {rec.x, rec.y, rec.z};
+                    const float inv = ldexpf(1.0f, -fb);
+                    const int slot = ngs > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
+                    int bgv[3], lv[3];
+                    uint32_t par = 0;
+    #pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const int b0 = (int)(rw[a] >> fb);
+                        int bg;
+                        uint32_t dgq;
+                        cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
+                        float w[4];
+                        pcs_weights((float)dgq * inv, w);
+                        float4 wv = make_float4(w[0], w[1], w[2], w[3]);
+                        if (a == 2) {
+                            wv = make_float4(wv.x * fscale, wv.y * fscale, wv.z * fscale, wv.w * fscale);
+                            par = (uint32_t)(bg - b0) & 1u;
+                            if (par) wv = make_float4(wv.y, wv.x, wv.w, wv.z);  // k cells in the order s ^ 1
+                        }
+                        sb.w[a][slot] = wv;
+                        // local index of the first stencil cell (periodic images
+                        // folded to the nearest copy of the tile)
+                        int l = bg - 1 - ts.t0[a];
+                        l -= l > Ng / 2 ? Ng : 0;
+                        l += l < -Ng / 2 ? Ng : 0;
+                        bgv[a] = bg;
+                        lv[a] = l;
+                    }
+                    const bool kmiss = !cyc[2] && (lv[2] < -3 || lv[2] >= ts.te[2]);  // stencil misses the tile
+                    uint4 loc;
+                    if (fast) {
+                        const uint32_t mi = (unsigned)(lv[0] + 4) < 40u ? masktab[0][lv[0] + 4] : 0u;
+                        const uint32_t mj = (unsigned)(lv[1] + 4) < 40u ? masktab[1][lv[1] + 4] : 0u;
+                        const int b0 = gofs + lv[0] * kSI + lv[1] * kSJ + lv[2] + kPadK + (int)par;
+                        loc = make_uint4((uint32_t)b0, (uint32_t)(b0 + 1 - 2 * (int)par), kmiss ? 0u : mi * mj, 0u);
+                    } else {
+                        uint32_t li, lj, lk;
+                        li = cyc[0] ? pack_local(bgv[0], Ng, ts.t0[0], ts.te[0], kOut)
+                                    : ((unsigned)(lv[0] + 4) < 40u ? loctab[0][lv[0] + 4] : 0xFFFFFFFFu);
+                        lj = cyc[1] ? pack_local(bgv[1], Ng, ts.t0[1], ts.te[1], kOut)
+                                    : ((unsigned)(lv[1] + 4) < 40u ? loctab[1][lv[1] + 4] : 0xFFFFFFFFu);
+                        if (cyc[2])
+                            lk = pack_local(bgv[2], Ng, ts.t0[2], ts.te[2], 0u) + 0x01010101u * kPadK;
+                        else
+                            lk = (uint32_t)(kmiss ? 0 : lv[2] + kPadK) * 0x01010101u + 0x03020100u;
+                        if (par) lk = ((lk & 0x00FF00FFu) << 8) | ((lk >> 8) & 0x00FF00FFu);
+                        loc = make_uint4(kmiss ? 0xFFFFFFFFu : li, lj, lk, 0u);
+                    }
+                    sb.loc[slot] = loc;
+                }
+                __syncwarp();
+                {
+                    const uint32_t qn = base + bstride + (lane & (parts - 1));
+                    if (qn < total) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
+                }
+                const int np = min((uint32_t)parts, total - base);
+                if (fast) {
+                    if (wide)
+                        deposit_all<true, true>(acc, sb, np, 1, lane);
+                    else
+                        deposit_all<false, true>(acc, sb, np, ngr, lane);
+                } else {
+                    if (wide)
+                        deposit_all<true, false>(acc, sb, np, 1, lane);
+                    else
+                        deposit_all<false, false>(acc, sb, np, ngr, lane);
+                }
+                __syncwarp();
+            }
+            __syncthreads();
 
-        // write the owned cells (and the row padding of the last k tile),
-        // clearing them for the next tile: warp w writes the i rows w, w + 16,
-        // ..., stepping along j with pointer increments; lanes along k
-        {
-            const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
-            const int rowlen = ts.te[2] + (last_k ? pp.Ng_pad - Ng : 0);
-            const int te1 = ts.te[1], te2 = ts.te[2];
-            const long rstride = (long)pp.Ng_pad;  // global floats between consecutive j
-            const long istride = rstride * Ng;     // and between consecutive i
-            const double s0 = po.ds ? po.ds->scale[0] : po.scale[0], s1 = po.ds ? po.ds->scale[1] : po.scale[1];
-            const float sc0 = (float)ldexp(s0, fixed ? -fixbits : 0);
-            const float sc1 = ngr > 1 ? (float)ldexp(s1, fixed ? -fixbits : 0) : 0.f;
-            const long obase = ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
-            for (int li = warp; li < ts.te[0]; li += nwarp) {
-                float *o0 = reinterpret_cast<float *>(po.out[0]) + obase + li * istride;
-                float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
-                uint32_t *a0 = acc + kPadK + li * kSI;
-                uint32_t *a1 = a0 + kGS;
-                for (int lj = 0; lj < te1; ++lj, o0 += rstride, o1 += rstride, a0 += kSJ, a1 += kSJ) {
-                    // padding cells take 0 x scale, as the reference scales the
-                    // whole padded grid (src/fft.c:127-129): NaN for an empty catalog
-                    float v0 = 0.f * sc0, v1 = 0.f * sc1;
-                    if (lane < te2) {
-                        const uint32_t c0 = a0[lane];
-                        a0[lane] = 0u;
-                        v0 = (fixed ? __uint2float_rn(c0) : __uint_as_float(c0)) * sc0;
-                        if (ngr > 1) {
-                            const uint32_t c1 = a1[lane];
-                            a1[lane] = 0u;
-                            v1 = (fixed ? __uint2float_rn(c1) : __uint_as_float(c1)) * sc1;
+            // the next tile's segments, loaded now and published after the write-out
+            if (pass == npass - 1 && next < ntiles) nb_comb = tile_segment(pp, off, next, tid, nb_begin, nb_cnt);
+
+            // write the owned cells (and the row padding of the last k tile),
+            // clearing them for the next tile: warp w writes the i rows w, w + 16,
+            // ..., stepping along j with pointer increments; lanes along k
+            {
+                const bool last_k = (ts.t0[2] + ts.te[2] == Ng);
+                const int rowlen = ts.te[2] + (last_k ? pp.Ng_pad - Ng : 0);
+                const int te1 = ts.te[1], te2 = ts.te[2];
+                const long rstride = (long)pp.Ng_pad;  // global floats between consecutive j
+                const long istride = rstride * Ng;     // and between consecutive i
+                const double s0 = po.ds ? po.ds->scale[0] : po.scale[0], s1 = po.ds ? po.ds->scale[1] : po.scale[1];
+                const long obase = ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
+                if (wide) {
+                    // grid `pass` from the 64-bit sums, then clear them all
+                    const double scd = ldexp(pass == 0 ? s0 : s1, -kWideBits);
+                    const float scf = (float)scd;
+                    const int accu = po.accumulate[pass];
+                    const unsigned long long *acc64 = reinterpret_cast<const unsigned long long *>(acc);
+                    for (int li = warp; li < ts.te[0]; li += nwarp) {
+                        float *o = reinterpret_cast<float *>(po.out[pass]) + obase + li * istride;
+                        const unsigned long long *a = acc64 + kPadK + li * kSI;
+                        for (int lj = 0; lj < te1; ++lj, o += rstride, a += kSJ) {
+                            float v = 0.f * scf;
+                            if (lane < te2) v = (float)((double)a[lane] * scd);
+                            if (lane < rowlen) {
+                                if (!accu) o[lane] = v;
+                                else if (lane < te2) o[lane] += v;
+                            }
+                            if (lane + 32 < rowlen && !accu) o[lane + 32] = 0.f * scf;
                         }
                     }
-                    if (lane < rowlen) {
-                        if (!po.accumulate[0]) o0[lane] = v0;
-                        else if (lane < te2) o0[lane] += v0;
-                        if (ngr > 1) {
-                            if (!po.accumulate[1]) o1[lane] = v1;
-                            else if (lane < te2) o1[lane] += v1;
+                    __syncthreads();
+                    for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
+                        reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
+                    __syncthreads();
+                    continue;
+                }
+                const float sc0 = (float)ldexp(s0, -fixbits);
+                const float sc1 = ngr > 1 ? (float)ldexp(s1, -fixbits) : 0.f;
+                for (int li = warp; li < ts.te[0]; li += nwarp) {
+                    float *o0 = reinterpret_cast<float *>(po.out[0]) + obase + li * istride;
+                    float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
+                    uint32_t *a0 = acc + kPadK + li * kSI;
+                    uint32_t *a1 = a0 + kGS;
+                    for (int lj = 0; lj < te1; ++lj, o0 += rstride, o1 += rstride, a0 += kSJ, a1 += kSJ) {
+                        // padding cells take 0 x scale, as the reference scales the
+                        // whole padded grid (src/fft.c:127-129): NaN for an empty catalog
+                        float v0 = 0.f * sc0, v1 = 0.f * sc1;
+                        if (lane < te2) {
+                            const uint32_t c0 = a0[lane];
+                            a0[lane] = 0u;
+                            v0 = __uint2float_rn(c0) * sc0;
+                            if (ngr > 1) {
+                                const uint32_t c1 = a1[lane];
+                                a1[lane] = 0u;
+                                v1 = __uint2float_rn(c1) * sc1;
+                            }
                         }
-                    }
-                    if (lane + 32 < rowlen) {  // row padding beyond a full 32-cell tile
-                        if (!po.accumulate[0]) o0[lane + 32] = 0.f * sc0;
-                        if (ngr > 1 && !po.accumulate[1]) o1[lane + 32] = 0.f * sc1;
+                        if (lane < rowlen) {
+                            if (!po.accumulate[0]) o0[lane] = v0;
+                            else if (lane < te2) o0[lane] += v0;
+                            if (ngr > 1) {
+                                if (!po.accumulate[1]) o1[lane] = v1;
+                                else if (lane < te2) o1[lane] += v1;
+                            }
+                        }
+                        if (lane + 32 < rowlen) {  // row padding beyond a full 32-cell tile
+                            if (!po.accumulate[0]) o0[lane + 32] = 0.f * sc0;
+                            if (ngr > 1 && !po.accumulate[1]) o1[lane + 32] = 0.f * sc1;
+                        }
                     }
                 }
             }
