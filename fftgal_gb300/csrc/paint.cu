@@ -613,6 +613,97 @@ __device__ __forceinline__ int fix_bits_for(uint32_t n) {
     return fb > kMaxFixBits ? kMaxFixBits : fb;
 }
 
+// Pass B over the tile's records: each warp stages 16 particles for both
+// grids (NGS = 2: lanes 0..15 grid 0, 16..31 grid 1) or 32 particles of grid
+// g1 (NGS = 1), then deposits them, into 32-bit sums or (WIDE) the 64-bit sums
+// of grid g1; the records of the warp's next batch are loaded before the
+// deposit so their latency hides behind it
+template <int NGS, bool WIDE>
+__device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const uint4 *__restrict__ sorted,
+                                              const uint32_t *seg_begin, const uint32_t *seg_pref,
+                                              const TileSegs &ts, const PaintParams &pp, const bool *cyc,
+                                              bool fast, float fscale, int g1, const uint32_t (*loctab)[40],
+                                              const uint32_t (*masktab)[40], int lane, int warp) {
+    const int Ng = pp.Ng, fb = pp.fb, nseg = ts.nseg;
+    const uint32_t total = ts.total;
+    constexpr int nwarp = kPaintThreads / 32;
+    const int parts = NGS > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
+    const int gs = NGS > 1 ? lane / kStageParts : g1;             // the grid this lane stages
+    const int gofs = WIDE ? 0 : gs * kGS;                         // and its accumulator
+    const uint32_t bstride = (uint32_t)nwarp * parts;
+    uint32_t base = (uint32_t)warp * parts;
+    uint4 rec = make_uint4(0, 0, 0, 0);
+    {
+        const uint32_t q = base + (lane & (parts - 1));
+        if (q < total) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
+    }
+    for (; base < total; base += bstride) {
+        const uint32_t q = base + (lane & (parts - 1));
+        if (q < total) {
+            const uint32_t rw[3] = {rec.x, rec.y, rec.z};
+            const float inv = ldexpf(1.0f, -fb);
+            const int slot = NGS > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
+            int bgv[3], lv[3];
+            uint32_t par = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const int b0 = (int)(rw[a] >> fb);
+                int bg;
+                uint32_t dgq;
+                cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
+                float w[4];
+                pcs_weights((float)dgq * inv, w);
+                float4 wv = make_float4(w[0], w[1], w[2], w[3]);
+                if (a == 2) {
+                    wv = make_float4(wv.x * fscale, wv.y * fscale, wv.z * fscale, wv.w * fscale);
+                    par = (uint32_t)(bg - b0) & 1u;
+                    if (par) wv = make_float4(wv.y, wv.x, wv.w, wv.z);  // k cells in the order s ^ 1
+                }
+                sb.w[a][slot] = wv;
+                // local index of the first stencil cell (periodic images
+                // folded to the nearest copy of the tile)
+                int l = bg - 1 - ts.t0[a];
+                l -= l > Ng / 2 ? Ng : 0;
+                l += l < -Ng / 2 ? Ng : 0;
+                bgv[a] = bg;
+                lv[a] = l;
+            }
+            const bool kmiss = !cyc[2] && (lv[2] < -3 || lv[2] >= ts.te[2]);  // stencil misses the tile
+            uint4 loc;
+            if (fast) {
+                const uint32_t mi = (unsigned)(lv[0] + 4) < 40u ? masktab[0][lv[0] + 4] : 0u;
+                const uint32_t mj = (unsigned)(lv[1] + 4) < 40u ? masktab[1][lv[1] + 4] : 0u;
+                const int b0 = gofs + lv[0] * kSI + lv[1] * kSJ + lv[2] + kPadK + (int)par;
+                loc = make_uint4((uint32_t)b0, (uint32_t)(b0 + 1 - 2 * (int)par), kmiss ? 0u : mi * mj, 0u);
+            } else {
+                uint32_t li, lj, lk;
+                li = cyc[0] ? pack_local(bgv[0], Ng, ts.t0[0], ts.te[0], kOut)
+                            : ((unsigned)(lv[0] + 4) < 40u ? loctab[0][lv[0] + 4] : 0xFFFFFFFFu);
+                lj = cyc[1] ? pack_local(bgv[1], Ng, ts.t0[1], ts.te[1], kOut)
+                            : ((unsigned)(lv[1] + 4) < 40u ? loctab[1][lv[1] + 4] : 0xFFFFFFFFu);
+                if (cyc[2])
+                    lk = pack_local(bgv[2], Ng, ts.t0[2], ts.te[2], 0u) + 0x01010101u * kPadK;
+                else
+                    lk = (uint32_t)(kmiss ? 0 : lv[2] + kPadK) * 0x01010101u + 0x03020100u;
+                if (par) lk = ((lk & 0x00FF00FFu) << 8) | ((lk >> 8) & 0x00FF00FFu);
+                loc = make_uint4(kmiss ? 0xFFFFFFFFu : li, lj, lk, 0u);
+            }
+            sb.loc[slot] = loc;
+        }
+        __syncwarp();
+        {
+            const uint32_t qn = base + bstride + (lane & (parts - 1));
+            if (qn < total) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
+        }
+        const int np = min((uint32_t)parts, total - base);
+        if (fast)
+            deposit_all<WIDE, true>(acc, sb, np, NGS, lane);
+        else
+            deposit_all<WIDE, false>(acc, sb, np, NGS, lane);
+        __syncwarp();
+    }
+}
+
 // Persistent: each CTA paints tiles blockIdx.x, blockIdx.x + gridDim.x, ...
 // The next tile's segment offsets are loaded during the write-out, the
 // accumulators are cleared as they are written out, and each warp loads its
@@ -763,7 +854,6 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         const bool wide = fixbits < kWideBelow;
         const int npass = wide ? ngr : 1;
         const float fscale = ldexpf(1.0f, wide ? kWideBits : fixbits);
-        const int ngs = wide ? 1 : ngr;  // grids staged per round
         if (wide) {
             // the 32-bit tiles leave sums in the row padding: clear all of it
             __syncthreads();
@@ -776,93 +866,12 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         uint32_t nb_begin = 0, nb_cnt = 0;
         int nb_comb = 0;
         for (int pass = 0; pass < npass; ++pass) {
-            // pass B: each warp stages 16 particles for both grids (lanes 0..15
-            // grid 0, 16..31 grid 1), or 32 particles for one grid, then deposits
-            // them; the records of the warp's next batch are loaded before the
-            // deposit so their latency hides behind it
-            StageBuf &sb = stage[warp];
-            const int parts = ngs > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
-            const int gs = ngs > 1 ? lane / kStageParts : pass;           // the grid this lane stages
-            const int gofs = wide ? 0 : gs * kGS;                         // and its accumulator
-            const uint32_t bstride = (uint32_t)nwarp * parts;
-            uint32_t base = (uint32_t)warp * parts;
-            uint4 rec = make_uint4(0, 0, 0, 0);
-            {
-                const uint32_t q = base + (lane & (parts - 1));
-                if (q < total) rec = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
-            }
-            for (; base < total; base += bstride) {
-                const uint32_t q = base + (lane & (parts - 1));
-                if (q < total) {
-                    const uint32_t rw[3] = {rec.x, rec.y, rec.z};
-                    const float inv = ldexpf(1.0f, -fb);
-                    const int slot = ngs > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
-                    int bgv[3], lv[3];
-                    uint32_t par = 0;
-    #pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        const int b0 = (int)(rw[a] >> fb);
-                        int bg;
-                        uint32_t dgq;
-                        cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
-                        float w[4];
-                        pcs_weights((float)dgq * inv, w);
-                        float4 wv = make_float4(w[0], w[1], w[2], w[3]);
-                        if (a == 2) {
-                            wv = make_float4(wv.x * fscale, wv.y * fscale, wv.z * fscale, wv.w * fscale);
-                            par = (uint32_t)(bg - b0) & 1u;
-                            if (par) wv = make_float4(wv.y, wv.x, wv.w, wv.z);  // k cells in the order s ^ 1
-                        }
-                        sb.w[a][slot] = wv;
-                        // local index of the first stencil cell (periodic images
-                        // folded to the nearest copy of the tile)
-                        int l = bg - 1 - ts.t0[a];
-                        l -= l > Ng / 2 ? Ng : 0;
-                        l += l < -Ng / 2 ? Ng : 0;
-                        bgv[a] = bg;
-                        lv[a] = l;
-                    }
-                    const bool kmiss = !cyc[2] && (lv[2] < -3 || lv[2] >= ts.te[2]);  // stencil misses the tile
-                    uint4 loc;
-                    if (fast) {
-                        const uint32_t mi = (unsigned)(lv[0] + 4) < 40u ? masktab[0][lv[0] + 4] : 0u;
-                        const uint32_t mj = (unsigned)(lv[1] + 4) < 40u ? masktab[1][lv[1] + 4] : 0u;
-                        const int b0 = gofs + lv[0] * kSI + lv[1] * kSJ + lv[2] + kPadK + (int)par;
-                        loc = make_uint4((uint32_t)b0, (uint32_t)(b0 + 1 - 2 * (int)par), kmiss ? 0u : mi * mj, 0u);
-                    } else {
-                        uint32_t li, lj, lk;
-                        li = cyc[0] ? pack_local(bgv[0], Ng, ts.t0[0], ts.te[0], kOut)
-                                    : ((unsigned)(lv[0] + 4) < 40u ? loctab[0][lv[0] + 4] : 0xFFFFFFFFu);
-                        lj = cyc[1] ? pack_local(bgv[1], Ng, ts.t0[1], ts.te[1], kOut)
-                                    : ((unsigned)(lv[1] + 4) < 40u ? loctab[1][lv[1] + 4] : 0xFFFFFFFFu);
-                        if (cyc[2])
-                            lk = pack_local(bgv[2], Ng, ts.t0[2], ts.te[2], 0u) + 0x01010101u * kPadK;
-                        else
-                            lk = (uint32_t)(kmiss ? 0 : lv[2] + kPadK) * 0x01010101u + 0x03020100u;
-                        if (par) lk = ((lk & 0x00FF00FFu) << 8) | ((lk >> 8) & 0x00FF00FFu);
-                        loc = make_uint4(kmiss ? 0xFFFFFFFFu : li, lj, lk, 0u);
-                    }
-                    sb.loc[slot] = loc;
-                }
-                __syncwarp();
-                {
-                    const uint32_t qn = base + bstride + (lane & (parts - 1));
-                    if (qn < total) rec = sorted[seg_index(qn, seg_begin, seg_pref, nseg)];
-                }
-                const int np = min((uint32_t)parts, total - base);
-                if (fast) {
-                    if (wide)
-                        deposit_all<true, true>(acc, sb, np, 1, lane);
-                    else
-                        deposit_all<false, true>(acc, sb, np, ngr, lane);
-                } else {
-                    if (wide)
-                        deposit_all<true, false>(acc, sb, np, 1, lane);
-                    else
-                        deposit_all<false, false>(acc, sb, np, ngr, lane);
-                }
-                __syncwarp();
-            }
+            if (wide)
+                paint_records<1, true>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, pass,
+                                       loctab, masktab, lane, warp);
+            else
+                paint_records<NGR, false>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, 0,
+                                          loctab, masktab, lane, warp);
             __syncthreads();
 
             // the next tile's segments, loaded now and published after the write-out
