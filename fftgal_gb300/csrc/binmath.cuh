@@ -84,12 +84,8 @@ __device__ __forceinline__ int kbin_est(uint32_t n2, float kamp, const uint32_t 
 // grid axis with the smallest |n_a|): the run's sums of P L_l(mu^2), l = 0, 2,
 // 4, 6, and of P per wedge stay in registers and are added to the CTA's FP32
 // shared accumulators acc32 [4 + W][NK] when the bin or the wedge changes.
-// The bin's n^2 limits [lo, hi) stay in registers: a mode inside them keeps
-// the bin without the threshold search (a run crosses ~0.3 bin edges per mode).
 struct BinRun {
     int cb = -1, cm = -1;
-    int tb = -1;                   // bin of [lo, hi), -1 beyond the last bin
-    uint32_t lo = 1u, hi = 0u;     // empty until the first mode
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, sw = 0.f;
 
     __device__ __forceinline__ void flush_bin(float *acc32, int NK) {
@@ -110,19 +106,8 @@ struct BinRun {
         const float pc = (kraw != 0 && 2 * kraw != d.Ng) ? 2.f * p : p;
         const float n2f = (float)n2;
         const float rk = rsqrtf(n2f);
-        if (n2 < lo || n2 >= hi) {
-            const int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
-            if (b >= NK) {
-                tb = -1;
-                lo = thr[NK];
-                hi = 0xFFFFFFFFu;
-            } else {
-                tb = b;
-                lo = thr[b];
-                hi = thr[b + 1];
-            }
-        }
-        const int b = tb;
+        int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
+        if (b >= NK) b = -1;
         float m2;
         const int imu = wedge_index_r(ki, kj, kk, rk, d, m2);
         if (b != cb) {
