@@ -639,12 +639,14 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
     }
     for (; base < total; base += bstride) {
         const uint32_t q = base + (lane & (parts - 1));
-        if (q < total) {
+        const bool valid = q < total;
+        const int slot = NGS > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
+        int bgv[3] = {0, 0, 0}, lv[3] = {0, 0, 0};
+        uint32_t par = 0;
+        float4 wk = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) {
             const uint32_t rw[3] = {rec.x, rec.y, rec.z};
             const float inv = ldexpf(1.0f, -fb);
-            const int slot = NGS > 1 ? stage_slot(lane & (kStageParts - 1), gs) : lane;
-            int bgv[3], lv[3];
-            uint32_t par = 0;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const int b0 = (int)(rw[a] >> fb);
@@ -653,13 +655,12 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
                 cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
                 float w[4];
                 pcs_weights((float)dgq * inv, w);
-                float4 wv = make_float4(w[0], w[1], w[2], w[3]);
                 if (a == 2) {
-                    wv = make_float4(wv.x * fscale, wv.y * fscale, wv.z * fscale, wv.w * fscale);
+                    wk = make_float4(w[0] * fscale, w[1] * fscale, w[2] * fscale, w[3] * fscale);
                     par = (uint32_t)(bg - b0) & 1u;
-                    if (par) wv = make_float4(wv.y, wv.x, wv.w, wv.z);  // k cells in the order s ^ 1
+                } else {
+                    sb.w[a][slot] = make_float4(w[0], w[1], w[2], w[3]);
                 }
-                sb.w[a][slot] = wv;
                 // local index of the first stencil cell (periodic images
                 // folded to the nearest copy of the tile)
                 int l = bg - 1 - ts.t0[a];
@@ -668,6 +669,19 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
                 bgv[a] = bg;
                 lv[a] = l;
             }
+        }
+        if (NGS == 1) {
+            // one grid: the half warps deposit particles 2m and 2m + 1 together.
+            // A first cell's bank parity is that of lv[2] + kPadK (the row
+            // offsets kSI, kSJ are even), so particle 2m + 1 takes its k cells in
+            // the order s ^ par that puts the pair's cells of every step in banks
+            // of opposite parity, 16 distinct banks each: one wavefront per step
+            const int other = __shfl_xor_sync(0xffffffffu, lv[2], 1);
+            par = (lane & 1) ? (uint32_t)(((lv[2] ^ other) & 1) ^ 1) : 0u;
+        }
+        if (valid) {
+            if (par) wk = make_float4(wk.y, wk.x, wk.w, wk.z);  // k cells in the order s ^ 1
+            sb.w[2][slot] = wk;
             const bool kmiss = !cyc[2] && (lv[2] < -3 || lv[2] >= ts.te[2]);  // stencil misses the tile
             uint4 loc;
             if (fast) {
