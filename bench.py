@@ -445,11 +445,22 @@ def learned_leg(args, fg, grid, stream, barrier, ptrs, Np, dK, ms_interlaced, re
         barrier()
         ms = e0.elapsed_time(e1) / args.steps
         out[name] = {"catalogs_per_s": 1000.0 / ms, "ms_per_step": ms, "result": r}
+        # stage times of three more calls, outside the timed region
+        grid.set_timing(True)
+        st = {k: [] for k in fg.STAGES}
+        for _ in range(3):
+            fn()
+            for k, v in grid.stage_times().items():
+                st[k].append(v)
+        grid.set_timing(False)
+        out[name]["stages_ms"] = {k: round(float(np.median(v)), 4) for k, v in st.items()
+                                  if float(np.median(v)) > 0.005}
     Ng = grid.Ng
     summary = {
         "catalogs_per_s": out["learned"]["catalogs_per_s"],
         "speedup_vs_interlaced": ms_interlaced / out["learned"]["ms_per_step"],
         "single_paint_catalogs_per_s": out["single_paint"]["catalogs_per_s"],
+        "stages_ms": {"learned": out["learned"]["stages_ms"], "single_paint": out["single_paint"]["stages_ms"]},
         "params": "fftgal_gb300/alias_mlp_params.npy",
     }
     if not (args.mock == "uniform" and Ng == NG and Np == NP and os.path.exists(GOLDEN)):
