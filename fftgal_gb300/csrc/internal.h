@@ -133,6 +133,10 @@ struct PaintTiling {
     int tab_off[3] = {0, 0, 0};   // offset of axis a's tables in d_tables
     long nkeys = 0;               // nt0*nt1*nt2 * 27
     int cta_per_sm = 0;           // persistent FP32 tile-paint CTAs per SM (1 or 2; 0: built-in 2)
+    // tiles of up to 32 x 16 x 32 cells for FP32 paints of one grid (owned;
+    // null where Ng < 64): the one grid's accumulators fill the shared memory
+    // that two grids of 16 x 16 x 32 take
+    PaintTiling *one = nullptr;
 };
 
 struct PaintScratch {

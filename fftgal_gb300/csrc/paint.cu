@@ -49,6 +49,7 @@
 namespace fg {
 
 constexpr int kTileExt[3] = {16, 16, 32};    // i, j, k
+constexpr int kTileExt1[3] = {32, 16, 32};   // FP32 paints of one grid (Ng >= 64)
 constexpr int kMaxPaintGrids = 2;
 // dense tiles (fewer 32-bit fraction bits than kWideBelow): 64-bit sums with
 // kWideBits fraction bits, one grid per pass
@@ -70,7 +71,11 @@ constexpr uint32_t kOut = 255u;
 static_assert(15 * kSI + 15 * kSJ + kSJ <= kGS, "tile does not fit the layout");
 static_assert(32 + 2 * kPadK <= kSJ, "row padding");
 static_assert(kSI % 32 == 8 && kSJ % 32 == 6 && kGS % 2 == 1, "bank layout");
-constexpr size_t kAccBytes = (sizeof(uint32_t) * 2 * kGS + 15) / 16 * 16;
+// the accumulators: two grids of 16 i rows, or one grid of 32 i rows (row li
+// at li * kSI)
+constexpr int kAccWords = 2 * kGS > 32 * kSI ? 2 * kGS : 32 * kSI;
+static_assert(31 * kSI + 15 * kSJ + kSJ <= kAccWords, "32-row tile does not fit the layout");
+constexpr size_t kAccBytes = (sizeof(uint32_t) * kAccWords + 15) / 16 * 16;
 // largest fixed-point scale: products stay below 2^22 so the FMA trick of
 // deposit4 converts them to integers exactly
 constexpr int kMaxFixBits = 23;
@@ -86,7 +91,7 @@ constexpr int kBlockCountBelow = 21;
 constexpr int kT3 = 16 * 16 * 32;
 // per-tile block counts: 4^3-cell blocks over the tile plus a 4-cell margin
 constexpr int kBlk = 4;
-__host__ __device__ constexpr int blk_dim(int a) { return a == 2 ? (32 + 8) / kBlk : (16 + 8) / kBlk; }  // 6, 6, 10
+__host__ __device__ constexpr int blk_dim(int a) { return a == 1 ? (16 + 8) / kBlk : (32 + 8) / kBlk; }  // 10, 6, 10
 constexpr int kBlkN = blk_dim(0) * blk_dim(1) * blk_dim(2);
 
 struct AxisParams {
@@ -575,7 +580,7 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
     } else {
         const uint32_t li = (loc.x >> (8 * a)) & 255u;
         const uint32_t lj = (loc.y >> (8 * b)) & 255u;
-        if ((li | lj) >= 16u) return;
+        if ((li | lj) >= 32u) return;  // kOut: a stencil row outside the tile
         const int row = g * kGS + (int)(li * kSI + lj * kSJ);
         dep_one<WIDE>(acc, row + (int)(loc.z & 255u), w, wz.x);
         dep_one<WIDE>(acc, row + (int)((loc.z >> 8) & 255u), w, wz.y);
@@ -731,7 +736,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                 // [2][kGS]
     StageBuf *stage = reinterpret_cast<StageBuf *>(smem_raw + kAccBytes);  // [warps]
-    uint32_t *blk = reinterpret_cast<uint32_t *>(stage + kPaintThreads / 32);  // [kBlkN]
+    // the per-block counts and their window sums (before pass B) use the stage area
+    uint32_t *blk = reinterpret_cast<uint32_t *>(stage) + kBlkN;  // [kBlkN]
+    static_assert(2 * kBlkN * sizeof(uint32_t) <= sizeof(StageBuf) * (kPaintThreads / 32), "block counts");
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
     __shared__ uint32_t scan_ws[32];
@@ -744,6 +751,26 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     // the j mask) set when stencil row a lies inside the tile
     __shared__ uint32_t masktab[2][40];
     int tab_te0 = -1, tab_te1 = -1;
+    // rebuild the tables for tile extents te0 x te1 (if they changed)
+    auto build_tabs = [&](int te0, int te1) {
+        if (te0 == tab_te0 && te1 == tab_te1) return;
+        __syncthreads();
+        if (threadIdx.x < 80) {
+            const int a = threadIdx.x / 40, l = threadIdx.x % 40 - 4, te = a == 0 ? te0 : te1;
+            uint32_t v = 0, m = 0;
+#pragma unroll
+            for (int s4 = 0; s4 < 4; ++s4) {
+                const bool in = (unsigned)(l + s4) < (unsigned)te;
+                v |= (in ? (uint32_t)(l + s4) : kOut) << (8 * s4);
+                m |= (in ? 1u : 0u) << (a == 0 ? 4 * s4 : s4);
+            }
+            loctab[a][l + 4] = v;
+            masktab[a][l + 4] = m;
+        }
+        __syncthreads();
+        tab_te0 = te0;
+        tab_te1 = te1;
+    };
 
     const int Ng = pp.Ng, ngr = NGR;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kPaintThreads / 32;  // launched with kPaintThreads
@@ -765,23 +792,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         bool cyc[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) cyc[a] = ts.te[a] == Ng;
-        if (ts.te[0] != tab_te0 || ts.te[1] != tab_te1) {
-            if (tid < 80) {
-                const int a = tid / 40, l = tid % 40 - 4, te = ts.te[a];
-                uint32_t v = 0, m = 0;
-#pragma unroll
-                for (int s4 = 0; s4 < 4; ++s4) {
-                    const bool in = (unsigned)(l + s4) < (unsigned)te;
-                    v |= (in ? (uint32_t)(l + s4) : kOut) << (8 * s4);
-                    m |= (in ? 1u : 0u) << (a == 0 ? 4 * s4 : s4);
-                }
-                loctab[a][l + 4] = v;
-                masktab[a][l + 4] = m;
-            }
-            __syncthreads();
-            tab_te0 = ts.te[0];
-            tab_te1 = ts.te[1];
-        }
+        build_tabs(ts.te[0], ts.te[1]);
 
         // fixed-point scale: the tile's particle total bounds every cell's
         // contributor count; only when that bound leaves fewer than
@@ -863,10 +874,12 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             __syncthreads();
             fixbits = fixbits_s;
         }
-        // a dense tile paints one grid per pass into 64-bit sums; otherwise
-        // one pass paints every grid into 32-bit sums
+        // a dense tile paints one grid per pass into 64-bit sums (one half of
+        // a 32-row tile at a time: 16 rows of 64-bit sums fill the shared
+        // memory); otherwise one pass paints every grid into 32-bit sums
         const bool wide = fixbits < kWideBelow;
-        const int npass = wide ? ngr : 1;
+        const int nhalf = (wide && ts.te[0] > 16) ? 2 : 1;
+        const int npass = wide ? ngr * nhalf : 1;
         const float fscale = ldexpf(1.0f, wide ? kWideBits : fixbits);
         if (wide) {
             // the 32-bit tiles leave sums in the row padding: clear all of it
@@ -880,8 +893,16 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         uint32_t nb_begin = 0, nb_cnt = 0;
         int nb_comb = 0;
         for (int pass = 0; pass < npass; ++pass) {
+            const int pg = pass / nhalf;  // the grid of a wide pass
+            TileSegs tv = ts;             // and its rows
+            if (nhalf == 2) {
+                const int ph = pass % nhalf;
+                tv.t0[0] = ts.t0[0] + 16 * ph;
+                tv.te[0] = ph ? ts.te[0] - 16 : 16;
+                build_tabs(tv.te[0], tv.te[1]);
+            }
             if (wide)
-                paint_records<1, true>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, pass,
+                paint_records<1, true>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
                                        loctab, masktab, lane, warp);
             else
                 paint_records<NGR, false>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, 0,
@@ -903,13 +924,14 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 const double s0 = po.ds ? po.ds->scale[0] : po.scale[0], s1 = po.ds ? po.ds->scale[1] : po.scale[1];
                 const long obase = ((long)ts.t0[0] * Ng + ts.t0[1]) * rstride + ts.t0[2];
                 if (wide) {
-                    // grid `pass` from the 64-bit sums, then clear them all
-                    const double scd = ldexp(pass == 0 ? s0 : s1, -kWideBits);
+                    // grid pg's rows of this pass from the 64-bit sums, then clear them all
+                    const double scd = ldexp(pg == 0 ? s0 : s1, -kWideBits);
                     const float scf = (float)scd;
-                    const int accu = po.accumulate[pass];
+                    const int accu = po.accumulate[pg];
                     const unsigned long long *acc64 = reinterpret_cast<const unsigned long long *>(acc);
-                    for (int li = warp; li < ts.te[0]; li += nwarp) {
-                        float *o = reinterpret_cast<float *>(po.out[pass]) + obase + li * istride;
+                    const long vbase = ((long)tv.t0[0] * Ng + tv.t0[1]) * rstride + tv.t0[2];
+                    for (int li = warp; li < tv.te[0]; li += nwarp) {
+                        float *o = reinterpret_cast<float *>(po.out[pg]) + vbase + li * istride;
                         const unsigned long long *a = acc64 + kPadK + li * kSI;
                         for (int lj = 0; lj < te1; ++lj, o += rstride, a += kSJ) {
                             float v = 0.f * scf;
@@ -1040,11 +1062,11 @@ paint_tile_f64_kernel(PaintParams pp, const uint32_t *__restrict__ off,
 
 // ---- host side -----------------------------------------------------------------------------
 
-int paint_tiling_create(PaintTiling *t, int Ng) {
+static int tiling_build(PaintTiling *t, int Ng, const int ext[3]) {
     std::vector<int> tab;
     long nk = 27;
     for (int a = 0; a < 3; ++a) {
-        int nt = (int)ceil_div(Ng, kTileExt[a]);
+        int nt = (int)ceil_div(Ng, ext[a]);
         // with more than one tile per axis every extent must be >= 5 so that a
         // stencil reaches at most the adjacent tile and the classes are exclusive
         while (nt > 1 && Ng / nt < 5) --nt;
@@ -1058,7 +1080,7 @@ int paint_tiling_create(PaintTiling *t, int Ng) {
             tmax = s1 - s0 > tmax ? s1 - s0 : tmax;
             for (int c = s0; c < s1; ++c) tab[base + c] = q;
         }
-        if (tmax > kTileExt[a]) return set_error(ERR_STATE, "paint tile extent %d > %d", tmax, kTileExt[a]);
+        if (tmax > ext[a]) return set_error(ERR_STATE, "paint tile extent %d > %d", tmax, ext[a]);
         t->nt[a] = nt;
         t->tmax[a] = tmax;
         nk *= nt;
@@ -1071,7 +1093,21 @@ int paint_tiling_create(PaintTiling *t, int Ng) {
     return OK;
 }
 
+int paint_tiling_create(PaintTiling *t, int Ng) {
+    FG_TRY(tiling_build(t, Ng, kTileExt));
+    if (Ng >= 64) {
+        t->one = new PaintTiling();
+        FG_TRY(tiling_build(t->one, Ng, kTileExt1));
+    }
+    return OK;
+}
+
 void paint_tiling_destroy(PaintTiling *t) {
+    if (t->one) {
+        paint_tiling_destroy(t->one);
+        delete t->one;
+        t->one = nullptr;
+    }
     cudaFree(t->d_tables);
     t->d_tables = nullptr;
 }
@@ -1122,6 +1158,8 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (ds && (grid_prec != 4 || pos_prec != 4)) return set_error(ERR_ARG, "paint: device scalars need FP32");
     if (rsd && rsd->v[0] && pos_prec != 4) return set_error(ERR_ARG, "paint: displacement needs FP32 positions");
     if (pos_prec != grid_prec) return set_error(ERR_ARG, "paint: position precision must match grid precision");
+    const int cta_per_sm = t->cta_per_sm;
+    if (ngrids == 1 && grid_prec == 4 && t->one) t = t->one;  // one FP32 grid: the 32 x 16 x 32 tiles
     if (Np < 0 || Np >= (1L << 32)) return set_error(ERR_ARG, "paint: Np out of range");
     for (int g = 1; g < ngrids; ++g)
         for (int a = 0; a < 3; ++a)
@@ -1201,10 +1239,10 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
     if (grid_prec == 4) {
-        const size_t smem = kAccBytes + sizeof(StageBuf) * (kPaintThreads / 32) + sizeof(uint32_t) * kBlkN;
+        const size_t smem = kAccBytes + sizeof(StageBuf) * (kPaintThreads / 32);
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        unsigned nb = (unsigned)((t->cta_per_sm == 1 ? 1 : 2) * num_sms());
+        unsigned nb = (unsigned)((cta_per_sm == 1 ? 1 : 2) * num_sms());
         nb = nb < ntiles ? nb : ntiles;
         if (ngrids == 1)
             paint_coop_kernel<1><<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);

@@ -498,20 +498,23 @@ def test_empty_and_wrapped_catalogs(fg, oracle_lib, prec, rel):
 
 
 @pytest.mark.parametrize("n_clump", [8_000, 200_000, 3_000_000])
-def test_dense_clump_fixed_point_scale(fg, oracle_lib, n_clump):
+@pytest.mark.parametrize("Ng,centre", [(32, (41.3, 57.9, 12.2)), (64, (25.1, 57.9, 12.2))])
+def test_dense_clump_fixed_point_scale(fg, oracle_lib, n_clump, Ng, centre):
     """A clump of n_clump particles inside one cell on top of 1e5 uniform ones.
     8000: the tile's 32-bit fixed-point sums keep 20 fraction bits (from the
     per-block count); 2e5 and 3e6 would leave 15 and 12, where the tiny
     products at the stencil's edge round to zero and bias the edge cells low
     (by up to 10 % of their value at 3e6), so the tile paints each grid into
-    64-bit sums with 22 fraction bits.  Against the FP64 oracle: the painted
+    64-bit sums with 22 fraction bits.  At Ng = 64 a single-grid paint uses
+    tiles of 32 i rows, whose 64-bit sums are painted one half at a time; the
+    clump's stencil there straddles the two halves.  Against the FP64 oracle: the painted
     grid within 5e-6 of its largest cell, every cell above 1e-4 of it within
     1e-3 of its own value, the total within 1e-6; the grid bit-reproducible;
     P_0,2,4 within the parity bound."""
-    Ng, L = 32, 100.0
+    L = 100.0
     rng = np.random.default_rng(n_clump)
     xu, yu, zu = uniform_box(9, 100_000, L)
-    c = np.array([41.3, 57.9, 12.2])
+    c = np.array(centre)
     clump = [c[a] + rng.uniform(-0.5, 0.5, n_clump) * (L / Ng) for a in range(3)]
     x, y, z = (np.concatenate([u, v]).astype(np.float32).astype(np.float64) for u, v in zip((xu, yu, zu), clump))
     V = L ** 3
