@@ -76,6 +76,20 @@ static_assert(kSI % 32 == 8 && kSJ % 32 == 6 && kGS % 2 == 1, "bank layout");
 constexpr int kAccWords = 2 * kGS > 32 * kSI ? 2 * kGS : 32 * kSI;
 static_assert(31 * kSI + 15 * kSJ + kSJ <= kAccWords, "32-row tile does not fit the layout");
 constexpr size_t kAccBytes = (sizeof(uint32_t) * kAccWords + 15) / 16 * 16;
+// two grids of 32 i rows (one 1024-thread CTA per SM): grid g at g * kGS2
+constexpr int kGS2 = 32 * kSI + 1;
+static_assert(31 * kSI + 15 * kSJ + kSJ <= kGS2 && kGS2 % 2 == 1, "32-row grid layout");
+
+// the tile-paint variants: 512 threads (two CTAs per SM) with the two grids
+// of 16 i rows at stride kGS (or one grid of 32 rows), or 1024 threads (one
+// CTA per SM) with two grids of 32 rows at stride kGS2
+template <int THREADS> struct PaintCfg;
+template <> struct PaintCfg<512> {
+    static constexpr int GS = kGS, ACC_WORDS = kAccWords, MINB = 2;
+};
+template <> struct PaintCfg<1024> {
+    static constexpr int GS = kGS2, ACC_WORDS = 2 * kGS2, MINB = 1;
+};
 // largest fixed-point scale: products stay below 2^22 so the FMA trick of
 // deposit4 converts them to integers exactly
 constexpr int kMaxFixBits = 23;
@@ -475,8 +489,8 @@ __device__ int tile_segment(const PaintParams &pp, const uint32_t *__restrict__ 
 __device__ void tile_publish(int ncomb, uint32_t b, uint32_t cnt, uint32_t *seg_begin, uint32_t *seg_pref,
                              uint32_t *scan_ws, TileSegs &ts) {
     const int q = threadIdx.x;
-    const uint32_t pref = block_exclusive_scan(cnt, scan_ws, &scan_ws[31]);
-    const uint32_t tot = scan_ws[31];
+    const uint32_t pref = block_exclusive_scan(cnt, scan_ws, &scan_ws[32]);  // scan_ws[33]
+    const uint32_t tot = scan_ws[32];
     if (q < ncomb) {
         seg_begin[q] = b;
         seg_pref[q] = pref;
@@ -563,7 +577,7 @@ __device__ __forceinline__ void dep_one(uint32_t *acc, int off, float w, float w
 // Otherwise loc.x / loc.y hold the 4 local i / j indices as bytes (kOut outside
 // the tile) and loc.z the 4 padded k cells as bytes, in step order.
 // The k weights are stored in step order.
-template <bool WIDE, bool FAST>
+template <bool WIDE, bool FAST, int GS>
 __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, int slot, int g, int a, int b,
                                             int lane_off) {
     const uint4 loc = sb.loc[slot];
@@ -581,7 +595,7 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
         const uint32_t li = (loc.x >> (8 * a)) & 255u;
         const uint32_t lj = (loc.y >> (8 * b)) & 255u;
         if ((li | lj) >= 32u) return;  // kOut: a stencil row outside the tile
-        const int row = g * kGS + (int)(li * kSI + lj * kSJ);
+        const int row = g * GS + (int)(li * kSI + lj * kSJ);
         dep_one<WIDE>(acc, row + (int)(loc.z & 255u), w, wz.x);
         dep_one<WIDE>(acc, row + (int)((loc.z >> 8) & 255u), w, wz.y);
         dep_one<WIDE>(acc, row + (int)((loc.z >> 16) & 255u), w, wz.z);
@@ -589,18 +603,18 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
     }
 }
 
-template <bool WIDE, bool FAST>
+template <bool WIDE, bool FAST, int GS>
 __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, int np, int ngr, int lane) {
     const int h = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
     const int lane_off = a * kSI + b * kSJ;
     if (ngr > 1) {
 #pragma unroll 4
-        for (int p = 0; p < np; ++p) deposit_one<WIDE, FAST>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
+        for (int p = 0; p < np; ++p) deposit_one<WIDE, FAST, GS>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
     } else {
         // one grid: 32 particles staged in slots 0..31, the half warps
         // deposit alternate ones
 #pragma unroll 2
-        for (int p = h; p < np; p += 2) deposit_one<WIDE, FAST>(acc, sb, p, 0, a, b, lane_off);
+        for (int p = h; p < np; p += 2) deposit_one<WIDE, FAST, GS>(acc, sb, p, 0, a, b, lane_off);
     }
 }
 
@@ -623,7 +637,7 @@ __device__ __forceinline__ int fix_bits_for(uint32_t n) {
 // g1 (NGS = 1), then deposits them, into 32-bit sums or (WIDE) the 64-bit sums
 // of grid g1; the records of the warp's next batch are loaded before the
 // deposit so their latency hides behind it
-template <int NGS, bool WIDE>
+template <int NGS, bool WIDE, int THREADS>
 __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const uint4 *__restrict__ sorted,
                                               const uint32_t *seg_begin, const uint32_t *seg_pref,
                                               const TileSegs &ts, const PaintParams &pp, const bool *cyc,
@@ -631,10 +645,10 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
                                               const uint32_t (*masktab)[40], int lane, int warp) {
     const int Ng = pp.Ng, fb = pp.fb, nseg = ts.nseg;
     const uint32_t total = ts.total;
-    constexpr int nwarp = kPaintThreads / 32;
+    constexpr int nwarp = THREADS / 32, GS = PaintCfg<THREADS>::GS;
     const int parts = NGS > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
     const int gs = NGS > 1 ? lane / kStageParts : g1;             // the grid this lane stages
-    const int gofs = WIDE ? 0 : gs * kGS;                         // and its accumulator
+    const int gofs = WIDE ? 0 : gs * GS;                          // and its accumulator
     const uint32_t bstride = (uint32_t)nwarp * parts;
     uint32_t base = (uint32_t)warp * parts;
     uint4 rec = make_uint4(0, 0, 0, 0);
@@ -716,9 +730,9 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
         }
         const int np = min((uint32_t)parts, total - base);
         if (fast)
-            deposit_all<WIDE, true>(acc, sb, np, NGS, lane);
+            deposit_all<WIDE, true, GS>(acc, sb, np, NGS, lane);
         else
-            deposit_all<WIDE, false>(acc, sb, np, NGS, lane);
+            deposit_all<WIDE, false, GS>(acc, sb, np, NGS, lane);
         __syncwarp();
     }
 }
@@ -729,19 +743,24 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
 // next batch of records before depositing the current one.
 // NGR = pp.ngrids (1 or 2), a template parameter so that the staging and
 // deposit loops are specialised for one grid or the interlaced pair.
-template <int NGR>
-__global__ void __launch_bounds__(kPaintThreads, 2)
+template <int NGR, int THREADS>
+__global__ void __launch_bounds__(THREADS, PaintCfg<THREADS>::MINB)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po, unsigned ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                 // [2][kGS]
-    StageBuf *stage = reinterpret_cast<StageBuf *>(smem_raw + kAccBytes);  // [warps]
+    constexpr int GS = PaintCfg<THREADS>::GS;
+    constexpr int ACC_BYTES = (4 * PaintCfg<THREADS>::ACC_WORDS + 15) / 16 * 16;
+    // rows of 64-bit sums that the accumulators hold (a dense tile's pass)
+    constexpr int WROWS = PaintCfg<THREADS>::ACC_WORDS / 2 / kSI;
+    static_assert(WROWS == 16 || WROWS == 32, "wide rows");
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                 // [2][GS]
+    StageBuf *stage = reinterpret_cast<StageBuf *>(smem_raw + ACC_BYTES);  // [warps]
     // the per-block counts and their window sums (before pass B) use the stage area
     uint32_t *blk = reinterpret_cast<uint32_t *>(stage) + kBlkN;  // [kBlkN]
-    static_assert(2 * kBlkN * sizeof(uint32_t) <= sizeof(StageBuf) * (kPaintThreads / 32), "block counts");
+    static_assert(2 * kBlkN * sizeof(uint32_t) <= sizeof(StageBuf) * (THREADS / 32), "block counts");
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
-    __shared__ uint32_t scan_ws[32];
+    __shared__ uint32_t scan_ws[33];
     __shared__ int fixbits_s;
     // packed local indices of the 4 stencil cells along i and j for a first
     // cell at l = -4 .. 35 relative to the tile start (kOut outside the tile);
@@ -773,10 +792,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     };
 
     const int Ng = pp.Ng, ngr = NGR;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kPaintThreads / 32;  // launched with kPaintThreads
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = THREADS / 32;  // launched with THREADS
     unsigned tile = blockIdx.x;
     if (tile >= ntiles) return;
-    for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
+    for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
         reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
     TileSegs ts;
     {
@@ -803,9 +822,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             int nb[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
-            for (int e = tid; e < kBlkN; e += kPaintThreads) blk[e] = 0u;
+            for (int e = tid; e < kBlkN; e += THREADS) blk[e] = 0u;
             __syncthreads();
-            for (uint32_t q = tid; q < total; q += kPaintThreads) {
+            for (uint32_t q = tid; q < total; q += THREADS) {
                 const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
                 const uint32_t rw[3] = {r.x, r.y, r.z};
                 int bidx = 0;
@@ -834,7 +853,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             // reuses the stage area.
             uint32_t *tmp = reinterpret_cast<uint32_t *>(stage);
             const int D1 = blk_dim(1), D2 = blk_dim(2);
-            for (int e = tid; e < kBlkN; e += kPaintThreads) {
+            for (int e = tid; e < kBlkN; e += THREADS) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 uint32_t v = 0;
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[2] || k + 2 < nb[2]);
@@ -843,7 +862,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 tmp[e] = v;
             }
             __syncthreads();
-            for (int e = tid; e < kBlkN; e += kPaintThreads) {
+            for (int e = tid; e < kBlkN; e += THREADS) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 uint32_t v = 0;
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[1] || j + 2 < nb[1]);
@@ -853,7 +872,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             }
             __syncthreads();
             uint32_t mx = 0;
-            for (int e = tid; e < kBlkN; e += kPaintThreads) {
+            for (int e = tid; e < kBlkN; e += THREADS) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[0] || i + 2 < nb[0]);
                 if (in) {
@@ -878,13 +897,13 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         // a 32-row tile at a time: 16 rows of 64-bit sums fill the shared
         // memory); otherwise one pass paints every grid into 32-bit sums
         const bool wide = fixbits < kWideBelow;
-        const int nhalf = (wide && ts.te[0] > 16) ? 2 : 1;
+        const int nhalf = (wide && ts.te[0] > WROWS) ? 2 : 1;
         const int npass = wide ? ngr * nhalf : 1;
         const float fscale = ldexpf(1.0f, wide ? kWideBits : fixbits);
         if (wide) {
             // the 32-bit tiles leave sums in the row padding: clear all of it
             __syncthreads();
-            for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
+            for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
                 reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
             __syncthreads();
         }
@@ -897,15 +916,15 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             TileSegs tv = ts;             // and its rows
             if (nhalf == 2) {
                 const int ph = pass % nhalf;
-                tv.t0[0] = ts.t0[0] + 16 * ph;
-                tv.te[0] = ph ? ts.te[0] - 16 : 16;
+                tv.t0[0] = ts.t0[0] + WROWS * ph;
+                tv.te[0] = ph ? ts.te[0] - WROWS : WROWS;
                 build_tabs(tv.te[0], tv.te[1]);
             }
             if (wide)
-                paint_records<1, true>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
+                paint_records<1, true, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
                                        loctab, masktab, lane, warp);
             else
-                paint_records<NGR, false>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, 0,
+                paint_records<NGR, false, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, 0,
                                           loctab, masktab, lane, warp);
             __syncthreads();
 
@@ -944,7 +963,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                         }
                     }
                     __syncthreads();
-                    for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
+                    for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
                         reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
                     __syncthreads();
                     continue;
@@ -955,7 +974,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                     float *o0 = reinterpret_cast<float *>(po.out[0]) + obase + li * istride;
                     float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
                     uint32_t *a0 = acc + kPadK + li * kSI;
-                    uint32_t *a1 = a0 + kGS;
+                    uint32_t *a1 = a0 + GS;
                     for (int lj = 0; lj < te1; ++lj, o0 += rstride, o1 += rstride, a0 += kSJ, a1 += kSJ) {
                         // padding cells take 0 x scale, as the reference scales the
                         // whole padded grid (src/fft.c:127-129): NaN for an empty catalog
@@ -1002,7 +1021,7 @@ paint_tile_f64_kernel(PaintParams pp, const uint32_t *__restrict__ off,
     double *acc = reinterpret_cast<double *>(smem_raw);  // [ngrids][kT3], dense [16][16][32]
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
-    __shared__ uint32_t scan_ws[32];
+    __shared__ uint32_t scan_ws[33];
     const int Ng = pp.Ng, ngr = pp.ngrids;
     for (int e = threadIdx.x; e < ngr * kT3; e += blockDim.x) acc[e] = 0.0;
     TileSegs ts;
@@ -1159,7 +1178,8 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     if (rsd && rsd->v[0] && pos_prec != 4) return set_error(ERR_ARG, "paint: displacement needs FP32 positions");
     if (pos_prec != grid_prec) return set_error(ERR_ARG, "paint: position precision must match grid precision");
     const int cta_per_sm = t->cta_per_sm;
-    if (ngrids == 1 && grid_prec == 4 && t->one) t = t->one;  // one FP32 grid: the 32 x 16 x 32 tiles
+    const bool big = grid_prec == 4 && t->one;  // FP32: the 32 x 16 x 32 tiles
+    if (big) t = t->one;
     if (Np < 0 || Np >= (1L << 32)) return set_error(ERR_ARG, "paint: Np out of range");
     for (int g = 1; g < ngrids; ++g)
         for (int a = 0; a < 3; ++a)
@@ -1238,16 +1258,28 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
-    if (grid_prec == 4) {
-        const size_t smem = kAccBytes + sizeof(StageBuf) * (kPaintThreads / 32);
-        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (grid_prec == 4 && ngrids == 2 && big) {
+        // two grids of 32-row tiles: one 1024-thread CTA per SM
+        constexpr int T = 1024;
+        const size_t smem = (4 * PaintCfg<T>::ACC_WORDS + 15) / 16 * 16 + sizeof(StageBuf) * (T / 32);
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        unsigned nb = (unsigned)num_sms();
+        nb = nb < ntiles ? nb : ntiles;
+        paint_coop_kernel<2, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+    } else if (grid_prec == 4) {
+        constexpr int T = kPaintThreads;
+        const size_t smem = kAccBytes + sizeof(StageBuf) * (T / 32);
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
         unsigned nb = (unsigned)((cta_per_sm == 1 ? 1 : 2) * num_sms());
         nb = nb < ntiles ? nb : ntiles;
         if (ngrids == 1)
-            paint_coop_kernel<1><<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+            paint_coop_kernel<1, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
         else
-            paint_coop_kernel<2><<<nb, kPaintThreads, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+            paint_coop_kernel<2, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
     } else {
         const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
         FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
