@@ -6,7 +6,8 @@
 // organisation is new:
 //
 //  1. count   : every particle gets the key (tile, class) of its base cell.  The
-//               grid is cut into tiles of at most 16 x 16 x 32 cells (i, j, k);
+//               grid is cut into tiles of at most 32 x 16 x 32 cells (i, j, k;
+//               FP32 grids with Ng >= 64) or 16 x 16 x 32 (FP64, smaller Ng);
 //               per axis the class says whether the particle's stencil (over
 //               all painted grids) reaches into the lower (1) or upper (2)
 //               neighbour tile, or neither (0).  Only the key histogram is
@@ -26,7 +27,9 @@
 // one particle (cell indices and the 3 x 4 weights of one grid) in shared
 // memory, then the warp deposits the particles one at a time with lane =
 // (grid, i row, j row), each lane adding its 4 k cells; the shared layout makes
-// every such step touch 32 distinct banks.  Sums are 32-bit fixed point with a
+// every such step touch 32 distinct banks.  Two interlacing grids of 32-row
+// tiles take 158 KB of sums: one 1024-thread CTA per SM; one grid of 32-row
+// tiles, or two of 16-row tiles, take 79 KB: two 512-thread CTAs per SM.  Sums are 32-bit fixed point with a
 // per-tile scale 2^-s, s the largest value for which no cell can exceed 2^32 (a
 // particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
 // total bounds every cell, and only where that bound leaves fewer than 21
