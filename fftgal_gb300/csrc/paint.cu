@@ -651,7 +651,7 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
     constexpr int nwarp = THREADS / 32, GS = PaintCfg<THREADS>::GS;
     const int parts = NGS > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
     const int gs = NGS > 1 ? lane / kStageParts : g1;             // the grid this lane stages
-    const int gofs = WIDE ? 0 : gs * GS;                          // and its accumulator
+    const int gofs = (WIDE || NGS == 1) ? 0 : gs * GS;            // and its accumulator
     const uint32_t bstride = (uint32_t)nwarp * parts;
     uint32_t base = (uint32_t)warp * parts;
     uint4 rec = make_uint4(0, 0, 0, 0);
@@ -749,7 +749,7 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
 template <int NGR, int THREADS>
 __global__ void __launch_bounds__(THREADS, PaintCfg<THREADS>::MINB)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
-                  PaintOut po, unsigned ntiles) {
+                  PaintOut po, unsigned ntiles, int gsplit) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int GS = PaintCfg<THREADS>::GS;
     constexpr int ACC_BYTES = (4 * PaintCfg<THREADS>::ACC_WORDS + 15) / 16 * 16;
@@ -796,7 +796,12 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
 
     const int Ng = pp.Ng, ngr = NGR;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = THREADS / 32;  // launched with THREADS
-    unsigned tile = blockIdx.x;
+    // gsplit (NGR = 1 with pp.ngrids = 2): even CTAs paint grid 0 and odd
+    // CTAs grid 1 of the same tiles, from one sort keyed for both grids
+    const int mg = (NGR == 1 && gsplit) ? (int)(blockIdx.x & 1) : 0;  // the grid of a one-grid CTA
+    const unsigned cta = (NGR == 1 && gsplit) ? blockIdx.x >> 1 : blockIdx.x;
+    const unsigned ncta = (NGR == 1 && gsplit) ? gridDim.x >> 1 : gridDim.x;
+    unsigned tile = cta;
     if (tile >= ntiles) return;
     for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
         reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
@@ -911,11 +916,11 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             __syncthreads();
         }
         const bool fast = !(cyc[0] || cyc[1] || cyc[2]);
-        const unsigned next = tile + gridDim.x;
+        const unsigned next = tile + ncta;
         uint32_t nb_begin = 0, nb_cnt = 0;
         int nb_comb = 0;
         for (int pass = 0; pass < npass; ++pass) {
-            const int pg = pass / nhalf;  // the grid of a wide pass
+            const int pg = NGR == 1 ? mg : pass / nhalf;  // the grid of a wide pass
             TileSegs tv = ts;             // and its rows
             if (nhalf == 2) {
                 const int ph = pass % nhalf;
@@ -927,8 +932,8 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 paint_records<1, true, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
                                        loctab, masktab, lane, warp);
             else
-                paint_records<NGR, false, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale, 0,
-                                          loctab, masktab, lane, warp);
+                paint_records<NGR, false, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale,
+                                                   mg, loctab, masktab, lane, warp);
             __syncthreads();
 
             // the next tile's segments, loaded now and published after the write-out
@@ -971,10 +976,12 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                     __syncthreads();
                     continue;
                 }
-                const float sc0 = (float)ldexp(s0, -fixbits);
+                // grid 0 here is the CTA's grid mg when it paints one grid
+                const float sc0 = (float)ldexp(mg ? s1 : s0, -fixbits);
                 const float sc1 = ngr > 1 ? (float)ldexp(s1, -fixbits) : 0.f;
+                const int accu0 = po.accumulate[mg];
                 for (int li = warp; li < ts.te[0]; li += nwarp) {
-                    float *o0 = reinterpret_cast<float *>(po.out[0]) + obase + li * istride;
+                    float *o0 = reinterpret_cast<float *>(po.out[mg]) + obase + li * istride;
                     float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
                     uint32_t *a0 = acc + kPadK + li * kSI;
                     uint32_t *a1 = a0 + GS;
@@ -993,7 +1000,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                             }
                         }
                         if (lane < rowlen) {
-                            if (!po.accumulate[0]) o0[lane] = v0;
+                            if (!accu0) o0[lane] = v0;
                             else if (lane < te2) o0[lane] += v0;
                             if (ngr > 1) {
                                 if (!po.accumulate[1]) o1[lane] = v1;
@@ -1001,7 +1008,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                             }
                         }
                         if (lane + 32 < rowlen) {  // row padding beyond a full 32-cell tile
-                            if (!po.accumulate[0]) o0[lane + 32] = 0.f * sc0;
+                            if (!accu0) o0[lane + 32] = 0.f * sc0;
                             if (ngr > 1 && !po.accumulate[1]) o1[lane + 32] = 0.f * sc1;
                         }
                     }
@@ -1261,28 +1268,28 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
     }
     if (ev) FG_CUDA(cudaEventRecord(ev[2], st));
     const unsigned ntiles = (unsigned)((long)t->nt[0] * t->nt[1] * t->nt[2]);
-    if (grid_prec == 4 && ngrids == 2 && big) {
-        // two grids of 32-row tiles: one 1024-thread CTA per SM
-        constexpr int T = 1024;
-        const size_t smem = (4 * PaintCfg<T>::ACC_WORDS + 15) / 16 * 16 + sizeof(StageBuf) * (T / 32);
-        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        unsigned nb = (unsigned)num_sms();
-        nb = nb < ntiles ? nb : ntiles;
-        paint_coop_kernel<2, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
-    } else if (grid_prec == 4) {
+    if (grid_prec == 4) {
+        // one grid per CTA where the tiles are 32 x 16 x 32: with two grids,
+        // even CTAs paint grid 0 and odd CTAs grid 1 (the sort's keys cover
+        // both grids' stencils); else both grids of 16-row tiles per CTA
         constexpr int T = kPaintThreads;
         const size_t smem = kAccBytes + sizeof(StageBuf) * (T / 32);
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
         FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
+        const int split = big && ngrids == 2;
         unsigned nb = (unsigned)((cta_per_sm == 1 ? 1 : 2) * num_sms());
-        nb = nb < ntiles ? nb : ntiles;
-        if (ngrids == 1)
-            paint_coop_kernel<1, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+        if (split) {
+            nb = nb < 2 * ntiles ? nb : 2 * ntiles;
+            nb &= ~1u;
+        } else {
+            nb = nb < ntiles ? nb : ntiles;
+        }
+        if (ngrids == 1 || split)
+            paint_coop_kernel<1, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles, split);
         else
-            paint_coop_kernel<2, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles);
+            paint_coop_kernel<2, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles, 0);
     } else {
         const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
         FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
