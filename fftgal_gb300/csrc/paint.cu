@@ -27,9 +27,10 @@
 // one particle (cell indices and the 3 x 4 weights of one grid) in shared
 // memory, then the warp deposits the particles one at a time with lane =
 // (grid, i row, j row), each lane adding its 4 k cells; the shared layout makes
-// every such step touch 32 distinct banks.  Two interlacing grids of 32-row
-// tiles take 158 KB of sums: one 1024-thread CTA per SM; one grid of 32-row
-// tiles, or two of 16-row tiles, take 79 KB: two 512-thread CTAs per SM.  Sums are 32-bit fixed point with a
+// every such step touch 32 distinct banks.  One grid of 32-row tiles, or two
+// of 16-row tiles, take 79 KB of sums: two 512-thread CTAs per SM.  The two
+// interlacing grids of 32-row tiles are painted by separate CTAs, one grid
+// each, from one sort.  Sums are 32-bit fixed point with a
 // per-tile scale 2^-s, s the largest value for which no cell can exceed 2^32 (a
 // particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
 // total bounds every cell, and only where that bound leaves fewer than 21
@@ -79,19 +80,13 @@ static_assert(kSI % 32 == 8 && kSJ % 32 == 6 && kGS % 2 == 1, "bank layout");
 constexpr int kAccWords = 2 * kGS > 32 * kSI ? 2 * kGS : 32 * kSI;
 static_assert(31 * kSI + 15 * kSJ + kSJ <= kAccWords, "32-row tile does not fit the layout");
 constexpr size_t kAccBytes = (sizeof(uint32_t) * kAccWords + 15) / 16 * 16;
-// two grids of 32 i rows (one 1024-thread CTA per SM): grid g at g * kGS2
-constexpr int kGS2 = 32 * kSI + 1;
-static_assert(31 * kSI + 15 * kSJ + kSJ <= kGS2 && kGS2 % 2 == 1, "32-row grid layout");
-
-// the tile-paint variants: 512 threads (two CTAs per SM) with the two grids
-// of 16 i rows at stride kGS (or one grid of 32 rows), or 1024 threads (one
-// CTA per SM) with two grids of 32 rows at stride kGS2
+// the tile-paint CTA shape: 512 threads, two CTAs per SM, the two grids of
+// 16 i rows at stride kGS or one grid of 32 rows.  (One 1024-thread CTA per
+// SM holding both grids of 32-row tiles, 158 KB of sums, was measured slower
+// than two one-grid CTAs per SM.)
 template <int THREADS> struct PaintCfg;
 template <> struct PaintCfg<512> {
     static constexpr int GS = kGS, ACC_WORDS = kAccWords, MINB = 2;
-};
-template <> struct PaintCfg<1024> {
-    static constexpr int GS = kGS2, ACC_WORDS = 2 * kGS2, MINB = 1;
 };
 // largest fixed-point scale: products stay below 2^22 so the FMA trick of
 // deposit4 converts them to integers exactly
