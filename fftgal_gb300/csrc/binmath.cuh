@@ -55,14 +55,15 @@ __device__ __forceinline__ int wedge_index(int ki, int kj, int kk, float kamp, c
     return (int)t;
 }
 
-// the same with mu = num * rsqrt(n2) (a few ulp; the tie band of
+// the same with mu = num * rsqrt(n2), num = k . los in FP32 in any order of
+// its three terms (a few ulp of the largest term; the tie band of
 // wedge_index covers it)
-__device__ __forceinline__ int wedge_index_r(int ki, int kj, int kk, float rkamp, const BinDev &d, float &mu2) {
+__device__ __forceinline__ int wedge_num_r(float num, int ki, int kj, int kk, float rkamp, const BinDev &d,
+                                           float &mu2) {
     if (d.zero_los) {
         mu2 = 0.f;
         return 0;
     }
-    const float num = (float)ki * d.l0f + (float)kj * d.l1f + (float)kk * d.l2f;
     const float mu = num * rkamp;
     mu2 = mu * mu;
     const float t = fabsf(mu * (float)d.Nmu);
@@ -70,6 +71,11 @@ __device__ __forceinline__ int wedge_index_r(int ki, int kj, int kk, float rkamp
     const float r = rintf(t);
     if (r >= 1.f && fabsf(t - r) < eps) return wedge_exact(ki, kj, kk, d);
     return (int)t;
+}
+
+__device__ __forceinline__ int wedge_index_r(int ki, int kj, int kk, float rkamp, const BinDev &d, float &mu2) {
+    const float num = (float)ki * d.l0f + (float)kj * d.l1f + (float)kk * d.l2f;
+    return wedge_num_r(num, ki, kj, kk, rkamp, d, mu2);
 }
 
 __device__ __forceinline__ int kbin_est(uint32_t n2, float kamp, const uint32_t *thr, int NK, float dKinv_f) {
@@ -101,15 +107,21 @@ struct BinRun {
     // 1 + (2 kraw % Ng > 0), src/power.c:57), power p; not the k = 0 mode
     __device__ __forceinline__ void add(const BinDev &d, const uint32_t *thr, float *acc32, int ki, int kj, int kk,
                                         int kraw, float p) {
-        const int NK = d.NK;
         const uint32_t n2 = (uint32_t)(ki * ki + kj * kj + kk * kk);
         const float pc = (kraw != 0 && 2 * kraw != d.Ng) ? 2.f * p : p;
+        const float num = (float)ki * d.l0f + (float)kj * d.l1f + (float)kk * d.l2f;
+        add_mode(d, thr, acc32, n2, num, pc, ki, kj, kk);
+    }
+    // the same with n^2, k . los (FP32) and the counted power pc given
+    __device__ __forceinline__ void add_mode(const BinDev &d, const uint32_t *thr, float *acc32, uint32_t n2,
+                                             float num, float pc, int ki, int kj, int kk) {
+        const int NK = d.NK;
         const float n2f = (float)n2;
         const float rk = rsqrtf(n2f);
         int b = kbin_est(n2, n2f * rk, thr, NK, d.dKinv_f);
         if (b >= NK) b = -1;
         float m2;
-        const int imu = wedge_index_r(ki, kj, kk, rk, d, m2);
+        const int imu = wedge_num_r(num, ki, kj, kk, rk, d, m2);
         if (b != cb) {
             flush_bin(acc32, NK);
             cb = b;
@@ -128,6 +140,45 @@ struct BinRun {
     }
     __device__ __forceinline__ void finish(const BinDev &d, float *acc32) { flush_bin(acc32, d.NK); }
 };
+
+// One thread's run of up to 16 modes along grid axis AX (0: i, 1: j, 2: k)
+// from mode (i, j, kc) (grid indices; kc < Ng/2 + 1), the t-th of whose
+// powers is p[t * ps]; the first n lie inside the half spectrum.  The two
+// fixed coordinates' parts of n^2 and of k . los are formed once per run.
+template <int AX>
+__device__ __forceinline__ void bin_run(const BinDev &d, const uint32_t *thr, float *acc32, int i, int j, int kc,
+                                        int n, const float *p, int ps) {
+    const int Ng = d.Ng;
+    BinRun run;
+    if (AX == 2) {
+        const int ki = kval(i, Ng), kj = kval(j, Ng);
+        const uint32_t n2c = (uint32_t)(ki * ki + kj * kj);
+        const float numc = (float)ki * d.l0f + (float)kj * d.l1f;
+        for (int t = 0; t < n; ++t) {
+            const int kr = kc + t, kk = kval(kr, Ng);
+            const uint32_t n2 = n2c + (uint32_t)(kk * kk);
+            if (n2 == 0) continue;  // the k = 0 mode (src/power.c:52-54)
+            const float pv = p[t * ps];
+            const float pc = (kr != 0 && 2 * kr != Ng) ? 2.f * pv : pv;
+            run.add_mode(d, thr, acc32, n2, numc + (float)kk * d.l2f, pc, ki, kj, kk);
+        }
+    } else {
+        const int kk = kval(kc, Ng), kf = kval(AX == 0 ? j : i, Ng);  // the fixed k and the other fixed index
+        const float fac = (kc != 0 && 2 * kc != Ng) ? 2.f : 1.f;
+        const uint32_t n2c = (uint32_t)(kk * kk + kf * kf);
+        const float numc = (float)kf * (AX == 0 ? d.l1f : d.l0f) + (float)kk * d.l2f;
+        const float lv = AX == 0 ? d.l0f : d.l1f;
+        const int v0 = AX == 0 ? i : j;
+        for (int t = 0; t < n; ++t) {
+            const int kv = kval(v0 + t, Ng);
+            const uint32_t n2 = n2c + (uint32_t)(kv * kv);
+            if (n2 == 0) continue;
+            run.add_mode(d, thr, acc32, n2, numc + (float)kv * lv, fac * p[t * ps], AX == 0 ? kv : kf,
+                         AX == 0 ? kf : kv, kk);
+        }
+    }
+    run.finish(d, acc32);
+}
 
 // fold a CTA's FP32 shared sums [NQ][NK] into the FP64 global sums [NK][NQ]
 // and clear them (every thread of the CTA takes part; the caller synchronises)

@@ -426,17 +426,18 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
         __syncwarp();
         if (fixed < Ng) {
             // runs along k: lane = (row, half of the 32 k); else lane = k
-            int r = axis == 2 ? (lane & 15) : 0, c = axis == 2 ? 16 * (lane >> 4) : lane;
-            const int dr = axis == 2 ? 0 : 1, dc = axis == 2 ? 1 : 0;
-            BinRun run;
-            for (int t = 0; t < 16; ++t, r += dr, c += dc) {
-                const int rr = r0 + r, kc = k0 + c;
-                if (rr >= Ng || kc >= kmain) continue;
-                const int i = rows_i ? rr : fixed, j = rows_i ? fixed : rr;
-                if ((i | j | kc) == 0) continue;  // the k = 0 mode (src/power.c:52-54)
-                run.add(d, thr, acc32, kval(i, Ng), kval(j, Ng), kval(kc, Ng), kc, slab[r * kSlabRow + c]);
+            if (axis == 2) {
+                const int r = lane & 15, c = 16 * (lane >> 4), rr = r0 + r, kc = k0 + c;
+                const int n = rr < Ng ? min(16, kmain - kc) : 0;
+                bin_run<2>(d, thr, acc32, fixed, rr, kc, n, slab + r * kSlabRow + c, 1);
+            } else {
+                const int kc = k0 + lane;
+                const int n = kc < kmain ? min(16, Ng - r0) : 0;
+                if (axis == 1)
+                    bin_run<1>(d, thr, acc32, fixed, r0, kc, n, slab + lane, kSlabRow);
+                else
+                    bin_run<0>(d, thr, acc32, r0, fixed, kc, n, slab + lane, kSlabRow);
             }
-            run.finish(d, acc32);
         }
         __syncwarp();
         if (++since_fold == fold) {
