@@ -410,16 +410,27 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
                 if (MODE == 2 || MODE == 5) pfk = cmul(fin.ph[(rows_i ? Ng : 0) + fixed], fin.ph[2 * Ng + k]);
                 wfk = fin.w[fixed] * fin.w[k] * fin.scale;
             }
+            // the row tables of the slab's 16 rows: lane r holds row r's, the
+            // loop takes them by shuffle
+            float2 phl = make_float2(0.f, 0.f);
+            float wl = 0.f;
+            if (MODE >= 2 && lane < kSlabJ && r0 + lane < Ng) {
+                if (MODE == 2 || MODE == 5) phl = fin.ph[(rows_i ? 0 : Ng) + r0 + lane];
+                wl = fin.w[r0 + lane];
+            }
+            const long estep = rows_i ? (long)Ng * nh : (long)nh;  // elements between consecutive rows
+            long e = (rows_i ? ((long)r0 * Ng + fixed) : ((long)fixed * Ng + r0)) * nh + k;
 #pragma unroll 4
-            for (int r = 0; r < kSlabJ; ++r) {
-                const int rr = r0 + r;
-                float pv = 0.f;
-                if (rr < Ng && k < kmain) {
-                    const long e = (rows_i ? ((long)rr * Ng + fixed) : ((long)fixed * Ng + rr)) * nh + k;
-                    const float2 phr = (MODE == 2 || MODE == 5) ? fin.ph[(rows_i ? 0 : Ng) + rr] : make_float2(0.f, 0.f);
-                    const float wr = MODE >= 2 ? fin.w[rr] : 0.f;
-                    pv = mode_power<MODE>(fin, f, e, pfk, phr, wfk, wr, Vinv, Pshot);
+            for (int r = 0; r < kSlabJ; ++r, e += estep) {
+                float2 phr = make_float2(0.f, 0.f);
+                float wr = 0.f;
+                if (MODE == 2 || MODE == 5) {
+                    phr.x = __shfl_sync(0xffffffffu, phl.x, r);
+                    phr.y = __shfl_sync(0xffffffffu, phl.y, r);
                 }
+                if (MODE >= 2) wr = __shfl_sync(0xffffffffu, wl, r);
+                float pv = 0.f;
+                if (r0 + r < Ng && k < kmain) pv = mode_power<MODE>(fin, f, e, pfk, phr, wfk, wr, Vinv, Pshot);
                 slab[r * kSlabRow + lane] = pv;
             }
         }
