@@ -431,7 +431,7 @@ struct TileSegs {
     uint32_t total;
 };
 
-__device__ __forceinline__ void tile_geometry(const PaintParams &pp, unsigned tile, TileSegs &ts) {
+__device__ void tile_geometry(const PaintParams &pp, unsigned tile, TileSegs &ts) {
     const int nt1 = pp.nt[1], nt2 = pp.nt[2];
     const int tt[3] = {(int)(tile / (nt1 * nt2)), (int)((tile / nt2) % nt1), (int)(tile % nt2)};
 #pragma unroll
@@ -443,7 +443,7 @@ __device__ __forceinline__ void tile_geometry(const PaintParams &pp, unsigned ti
 
 // thread q's segment of `tile` (q < the returned count): first sorted index b
 // and length cnt.  Issued a tile ahead so the loads overlap the write-out.
-__device__ __forceinline__ int tile_segment(const PaintParams &pp, const uint32_t *__restrict__ off, unsigned tile, int q,
+__device__ int tile_segment(const PaintParams &pp, const uint32_t *__restrict__ off, unsigned tile, int q,
                             uint32_t &b, uint32_t &cnt) {
     const int nt1 = pp.nt[1], nt2 = pp.nt[2];
     const int tt[3] = {(int)(tile / (nt1 * nt2)), (int)((tile / nt2) % nt1), (int)(tile % nt2)};
@@ -484,7 +484,7 @@ __device__ __forceinline__ int tile_segment(const PaintParams &pp, const uint32_
 }
 
 // publish the fetched segments in shared memory (every thread takes part)
-__device__ __forceinline__ void tile_publish(int ncomb, uint32_t b, uint32_t cnt, uint32_t *seg_begin, uint32_t *seg_pref,
+__device__ void tile_publish(int ncomb, uint32_t b, uint32_t cnt, uint32_t *seg_begin, uint32_t *seg_pref,
                              uint32_t *scan_ws, TileSegs &ts) {
     const int q = threadIdx.x;
     const uint32_t pref = block_exclusive_scan(cnt, scan_ws, &scan_ws[32]);  // scan_ws[33]
@@ -638,12 +638,9 @@ __device__ __forceinline__ int fix_bits_for(uint32_t n) {
 template <int NGS, bool WIDE, int THREADS>
 __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const uint4 *__restrict__ sorted,
                                               const uint32_t *seg_begin, const uint32_t *seg_pref,
-                                              const TileSegs ts, const PaintParams &pp, int cycm, bool fast,
-                                              float fscale, int g1, const uint32_t (*loctab)[40],
+                                              const TileSegs &ts, const PaintParams &pp, const bool *cyc,
+                                              bool fast, float fscale, int g1, const uint32_t (*loctab)[40],
                                               const uint32_t (*masktab)[40], int lane, int warp) {
-    // the tile geometry by value and the periodic axes as bits (cycm bit a:
-    // the tile spans axis a), so that nothing of them lives in local memory
-    const bool cyc[3] = {(cycm & 1) != 0, (cycm & 2) != 0, (cycm & 4) != 0};
     const int Ng = pp.Ng, fb = pp.fb, nseg = ts.nseg;
     const uint32_t total = ts.total;
     constexpr int nwarp = THREADS / 32, GS = PaintCfg<THREADS>::GS;
@@ -672,10 +669,7 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
                 const int b0 = (int)(rw[a] >> fb);
                 int bg;
                 uint32_t dgq;
-                // (no run-time index into the parameter space: it would copy the
-                // parameters to local memory)
-                const int dq = gs ? pp.ax[a].dq[1] : pp.ax[a].dq[0];
-                cell_g(b0, rw[a] & ((1u << fb) - 1), dq, fb, Ng, bg, dgq);
+                cell_g(b0, rw[a] & ((1u << fb) - 1), pp.ax[a].dq[gs], fb, Ng, bg, dgq);
                 float w[4];
                 pcs_weights((float)dgq * inv, w);
                 if (a == 2) {
@@ -917,7 +911,6 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             __syncthreads();
         }
         const bool fast = !(cyc[0] || cyc[1] || cyc[2]);
-        const int cycm = (cyc[0] ? 1 : 0) | (cyc[1] ? 2 : 0) | (cyc[2] ? 4 : 0);
         const unsigned next = tile + ncta;
         uint32_t nb_begin = 0, nb_cnt = 0;
         int nb_comb = 0;
@@ -931,10 +924,10 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 build_tabs(tv.te[0], tv.te[1]);
             }
             if (wide)
-                paint_records<1, true, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cycm, fast, fscale, pg,
+                paint_records<1, true, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
                                        loctab, masktab, lane, warp);
             else
-                paint_records<NGR, false, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cycm, fast, fscale,
+                paint_records<NGR, false, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale,
                                                    mg, loctab, masktab, lane, warp);
             __syncthreads();
 
@@ -956,11 +949,11 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                     // grid pg's rows of this pass from the 64-bit sums, then clear them all
                     const double scd = ldexp(pg == 0 ? s0 : s1, -kWideBits);
                     const float scf = (float)scd;
-                    const int accu = pg ? po.accumulate[1] : po.accumulate[0];
+                    const int accu = po.accumulate[pg];
                     const unsigned long long *acc64 = reinterpret_cast<const unsigned long long *>(acc);
                     const long vbase = ((long)tv.t0[0] * Ng + tv.t0[1]) * rstride + tv.t0[2];
                     for (int li = warp; li < tv.te[0]; li += nwarp) {
-                        float *o = reinterpret_cast<float *>(pg ? po.out[1] : po.out[0]) + vbase + li * istride;
+                        float *o = reinterpret_cast<float *>(po.out[pg]) + vbase + li * istride;
                         const unsigned long long *a = acc64 + kPadK + li * kSI;
                         for (int lj = 0; lj < te1; ++lj, o += rstride, a += kSJ) {
                             float v = 0.f * scf;
@@ -981,9 +974,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 // grid 0 here is the CTA's grid mg when it paints one grid
                 const float sc0 = (float)ldexp(mg ? s1 : s0, -fixbits);
                 const float sc1 = ngr > 1 ? (float)ldexp(s1, -fixbits) : 0.f;
-                const int accu0 = mg ? po.accumulate[1] : po.accumulate[0];
+                const int accu0 = po.accumulate[mg];
                 for (int li = warp; li < ts.te[0]; li += nwarp) {
-                    float *o0 = reinterpret_cast<float *>(mg ? po.out[1] : po.out[0]) + obase + li * istride;
+                    float *o0 = reinterpret_cast<float *>(po.out[mg]) + obase + li * istride;
                     float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
                     uint32_t *a0 = acc + kPadK + li * kSI;
                     uint32_t *a1 = a0 + GS;
