@@ -35,12 +35,12 @@
 // particle adds at most (2/3)^3 of its weight to a cell): the tile's particle
 // total bounds every cell, and only where that bound leaves fewer than 21
 // fraction bits does a first pass count particles per 4^3-cell block.  A tile
-// whose bound still leaves fewer than 20 bits (a dense clump: more than about
-// 14000 particles near one cell) paints one grid at a time into 64-bit sums
-// with 22 fraction bits over the same shared memory, since at 12-16 bits the
+// whose bound still leaves fewer than 16 bits (a dense clump: more than about
+// 2e5 particles near one cell) paints one grid at a time into 64-bit sums
+// with 22 fraction bits over the same shared memory, since at 12-15 bits the
 // many tiny products at a stencil's edge round to zero and bias the edge cells
-// low.  Integer sums are order independent, so the painted grid is
-// bit-reproducible run to run.
+// low by several percent.  Integer sums are order independent, so the painted
+// grid is bit-reproducible run to run.
 // FP64 grids (paint_tile_f64_kernel) reproduce the reference's FP64 weight
 // arithmetic op for op and accumulate in FP64, one thread per particle.
 #include "internal.h"
@@ -56,8 +56,12 @@ constexpr int kTileExt[3] = {16, 16, 32};    // i, j, k
 constexpr int kTileExt1[3] = {32, 16, 32};   // FP32 paints of one grid (Ng >= 64)
 constexpr int kMaxPaintGrids = 2;
 // dense tiles (fewer 32-bit fraction bits than kWideBelow): 64-bit sums with
-// kWideBits fraction bits, one grid per pass
-constexpr int kWideBelow = 20;
+// kWideBits fraction bits, one grid per pass.  At 16-19 bits the 32-bit sums
+// round the tiny products at a dense clump's stencil edge by up to 1.4 % of
+// those cells' values (1e-6 of the clump's peak cell, 1e-5 of its mass); the
+// clustered 1e8-galaxy lognormal mock has many such tiles, whose tile paint
+// the 64-bit passes took from 13.0 to 15.8 ms (Ng = 1024) at a threshold of 20
+constexpr int kWideBelow = 16;
 constexpr int kWideBits = 22;
 // FP32 shared layout: cell (li, lj, lk) of grid g at g*kGS + li*kSI + lj*kSJ +
 // kPadK + lk.  kSI = 8 and kSJ = 6 (mod 32) put the 16 rows (li+a, lj+b), a, b
