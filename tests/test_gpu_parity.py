@@ -497,7 +497,7 @@ def test_empty_and_wrapped_catalogs(fg, oracle_lib, prec, rel):
                 grid_close(np.array(g.f), np.array(o.f), rel)
 
 
-@pytest.mark.parametrize("n_clump,edge,mass", [(8_000, 2e-3, 2e-6), (50_000, 1e-2, 1e-5), (200_000, 1e-3, 1e-6),
+@pytest.mark.parametrize("n_clump,edge,mass", [(8_000, 2e-3, 2e-6), (50_000, 1e-2, 1e-5), (400_000, 1e-3, 1e-6),
                                                (3_000_000, 1e-3, 1e-6)])
 @pytest.mark.parametrize("Ng,centre", [(32, (41.3, 57.9, 12.2)), (64, (25.1, 57.9, 12.2))])
 def test_dense_clump_fixed_point_scale(fg, oracle_lib, n_clump, edge, mass, Ng, centre):
@@ -506,7 +506,7 @@ def test_dense_clump_fixed_point_scale(fg, oracle_lib, n_clump, edge, mass, Ng, 
     bits (from the per-block count), where rounding the tiny products at the
     stencil's edge to the nearest step biases the edge cells by up to 0.06 %
     and 0.3 % of their own value (a restatement of the rounding in numpy gives
-    those bounds); 2e5 and 3e6 would leave 15 and 12 bits, where the bias
+    those bounds); 4e5 and 3e6 would leave 15 and 12 bits, where the bias
     reaches several percent (10 % at 3e6), so the tile paints each grid into
     64-bit sums with 22 fraction bits.  At Ng = 64 a single-grid paint uses
     tiles of 32 i rows, whose 64-bit sums are painted one half at a time; the
