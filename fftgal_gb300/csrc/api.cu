@@ -487,9 +487,7 @@ static int tune_launch(fft_t *self, const char *path) {
                 }
             geo->cta_per_sm = t.bin_cta;
             geo->fold = t.bin_fold;
-            // tile paint on a uniform catalog, of the kernel whose CTAs per SM
-            // are tuned: the 512-thread one (one grid where Ng >= 64, whose
-            // two-grid paints run one 1024-thread CTA per SM; else both grids)
+            // tile paint of both interlacing grids on a uniform catalog
             long Np = (long)Ng * Ng * Ng / 10;
             Np = Np < 100000 ? 100000 : (Np > 200000000 ? 200000000 : Np);
             float *pos = nullptr;
@@ -513,7 +511,7 @@ static int tune_launch(fft_t *self, const char *path) {
                 double ms = 0;
                 rc = median_ms(st, [&]() {
                     return paint(&g->tiling, &g->scratch, 4, pos, pos + Np, pos + 2 * (size_t)Np, 4, Np,
-                                 Ng / self->L, spec, g->tiling.one ? 1 : 2, st);
+                                 Ng / self->L, spec, 2, st);
                 }, &ms);
                 if (rc != OK) break;
                 if (cta == 2) {
