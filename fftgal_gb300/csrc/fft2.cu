@@ -245,18 +245,24 @@ __device__ __forceinline__ void kr2c_tile(float *g, long nrows, int Ng_pad, int 
             for (int k2 = 0; k2 < N2; ++k2) S[r * P2 + k1 + N1 * k2] = res[q][k2];
     }
     __syncthreads();
-    // split into the half spectrum and store (lanes over consecutive k)
-    const int nh = M + 1;
-    for (int e = t; e < R * nh; e += nthr) {
-        const int r = e / nh, k = e - r * nh;
+    // split into the half spectrum and store (lanes over consecutive k): one
+    // pass over k = 0 .. M/2 forms X[k] = E + W^k O and, from the same E and
+    // W^k O, X[M - k] = conj(E - W^k O) (E[M-k] = conj(E[k]), O[M-k] = conj(O[k])
+    // and W^(M-k) = -conj(W^k) for W = exp(-2 pi i / 2M)); k = 0 also gives X[M]
+    constexpr int NPAIR = M / 2 + 1;
+    for (int e = t; e < R * NPAIR; e += nthr) {
+        const int r = e / NPAIR, k = e - r * NPAIR;
         if (row0 + r >= nrows) continue;
-        const int k1 = k == M ? 0 : k, k2 = k == 0 ? 0 : M - k;
-        const float2 z1 = S[r * P2 + k1];
-        const float2 z2 = cconj(S[r * P2 + k2]);
+        const int km = k == 0 ? 0 : M - k;
+        const float2 z1 = S[r * P2 + k];
+        const float2 z2 = cconj(S[r * P2 + km]);
         const float2 E = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y + z2.y));
         const float2 D = csub(z1, z2);
         const float2 O = make_float2(0.5f * D.y, -0.5f * D.x);
-        reinterpret_cast<float2 *>(g + (row0 + r) * Ng_pad)[k] = cadd(E, cmul(__ldg(&rtw[k]), O));
+        const float2 wo = cmul(__ldg(&rtw[k]), O);
+        float2 *out = reinterpret_cast<float2 *>(g + (row0 + r) * Ng_pad);
+        out[k] = cadd(E, wo);
+        if (k < M / 2) out[k == 0 ? M : M - k] = cconj(csub(E, wo));
     }
 }
 
