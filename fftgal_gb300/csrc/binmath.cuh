@@ -122,13 +122,23 @@ struct BinRun {
         if (b >= NK) b = -1;
         float m2;
         const int imu = wedge_num_r(num, ki, kj, kk, rk, d, m2);
-        if (b != cb) {
-            flush_bin(acc32, NK);
-            cb = b;
-            cm = imu;
-            s0 = s1 = s2 = s3 = sw = 0.f;
-        } else if (imu != cm) {
-            if (cb >= 0) atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
+        // one flush block for a new bin (all five sums) and a new wedge (its
+        // sum), so a warp whose lanes see both runs it once
+        const bool newbin = b != cb;
+        if (newbin || imu != cm) {
+            if (cb >= 0) {
+                if (newbin) {
+                    atomicAdd(acc32 + 0 * NK + cb, s0);
+                    atomicAdd(acc32 + 1 * NK + cb, s1);
+                    atomicAdd(acc32 + 2 * NK + cb, s2);
+                    atomicAdd(acc32 + 3 * NK + cb, s3);
+                }
+                atomicAdd(acc32 + (4 + cm) * NK + cb, sw);
+            }
+            if (newbin) {
+                cb = b;
+                s0 = s1 = s2 = s3 = 0.f;
+            }
             cm = imu;
             sw = 0.f;
         }
