@@ -124,30 +124,16 @@ __device__ __forceinline__ void cols_tile(float2 *base, int left, long es, int l
 
 template <int N1, int N2>
 __global__ void __launch_bounds__(512)
-fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC, long ntiles,
+fft2_cols_kernel(float2 *g0, float2 *g1, int ncols, long es, long bs, int logC,
                  const float2 *__restrict__ W, int sign) {
     extern __shared__ __align__(16) float2 S[];
     const int C = 1 << logC;
     const int ncb = (ncols + C - 1) >> logC;
+    const int cb = blockIdx.x % ncb;
+    const long batch = blockIdx.x / ncb;
     float2 *g = blockIdx.y == 0 ? g0 : g1;
-    // persistent over tiles: the next tile's rows are prefetched into L2 while
-    // this one is transformed, so its loads wait on L2 instead of HBM
-    for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long nxt = tile + gridDim.x;
-        if (nxt < ntiles) {
-            const int cn = (int)(nxt % ncb) << logC;
-            const int last = (ncols - cn < C ? ncols - cn : C) - 1;  // the last valid column
-            const float2 *nb = g + (nxt / ncb) * bs + cn;
-            for (int n = threadIdx.x; n < N1 * N2; n += blockDim.x) {
-                const float2 *p = nb + (long)n * es;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(p + last));
-            }
-        }
-        const int c0 = (int)(tile % ncb) << logC;
-        cols_tile<N1, N2>(g + (tile / ncb) * bs + c0, ncols - c0, es, logC, W, sign, S, threadIdx.x, blockDim.x);
-        __syncthreads();  // the next tile's step 1 rewrites S
-    }
+    const int c0 = cb << logC;
+    cols_tile<N1, N2>(g + batch * bs + c0, ncols - c0, es, logC, W, sign, S, threadIdx.x, blockDim.x);
 }
 
 // ---- strided axis of length 2048 = 32 x 64 ---------------------------------------------
@@ -643,13 +629,8 @@ bool fft2_supported(int Ng, int prec) {
     if (N1 == A && N2 == B) {                                                                             \
         FG_CUDA(cudaFuncSetAttribute(fft2_cols_kernel<A, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                      (int)smem));                                                         \
-        int per_sm = 0;                                                                                    \
-        FG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fft2_cols_kernel<A, B>, threads, smem)); \
-        const long ntiles = ncb * nbatch;                                                                  \
-        long nx = (long)(per_sm > 0 ? per_sm : 1) * num_sms() / ngrids;                                    \
-        nx = nx < 1 ? 1 : (nx > ntiles ? ntiles : nx);                                                     \
-        fft2_cols_kernel<A, B><<<dim3((unsigned)nx, ngrids), threads, smem, s>>>(                          \
-            (float2 *)g0, (float2 *)g1, ncols, es, bs, logC, ntiles, (const float2 *)W, sign);              \
+        fft2_cols_kernel<A, B><<<grid, threads, smem, s>>>((float2 *)g0, (float2 *)g1, ncols, es, bs,      \
+                                                           logC, (const float2 *)W, sign);                 \
         FG_LAUNCHED(1);                                                                                    \
         return OK;                                                                                         \
     }
