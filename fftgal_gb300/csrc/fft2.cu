@@ -36,27 +36,7 @@ __host__ __device__ constexpr int bitrev(int x, int bits) {
     return r;
 }
 
-// x * W_32^t (sign < 0) or x * conj(W_32^t) (sign > 0), W_32 = exp(-2 pi i / 32);
-// t is a compile-time constant after unrolling, so the quarter turns cost no
-// multiplication
-__device__ __forceinline__ float2 tw32_mul(float2 x, int t, int sign) {
-    t &= 31;
-    if (t == 0) return x;
-    if (t == 16) return make_float2(-x.x, -x.y);
-    if (t == 8) return cmul_si(x, sign);
-    if (t == 24) return cmul_si(x, -sign);
-    float2 w = c_w32[t];
-    if (sign > 0) w.y = -w.y;
-    return cmul(x, w);
-}
-
-// in-register FFT of length M <= 32, natural order in and out: bit-reversed
-// input, one radix-2 stage when log2 M is odd, then radix-4 stages.  A radix-4
-// stage fuses the radix-2 stages of half-spans h and 2h: with W = W_4h,
-//   A = x0, B = W^2j x1, C = W^j x2, D = W^3j x3 (x_q at s + j + q h),
-//   X_0 = (A+B) + (C+D), X_2h = (A+B) - (C+D),
-//   X_h = (A-B) + (sign i)(C-D), X_3h = (A-B) - (sign i)(C-D),
-// three twiddle products instead of the fused stages' four.
+// in-register radix-2 FFT of length M <= 32, natural order in and out
 template <int M>
 __device__ __forceinline__ void reg_fft(float2 (&v)[M], int sign) {
     if constexpr (M > 1) {
@@ -64,31 +44,24 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[M], int sign) {
         float2 a[M];
 #pragma unroll
         for (int i = 0; i < M; ++i) a[bitrev(i, B)] = v[i];
-        if constexpr (B % 2 == 1) {
 #pragma unroll
-            for (int s = 0; s < M; s += 2) {
-                const float2 u = a[s], t = a[s + 1];
-                a[s] = cadd(u, t);
-                a[s + 1] = csub(u, t);
-            }
-        }
+        for (int len = 2; len <= M; len <<= 1) {
+            const int h = len >> 1;
 #pragma unroll
-        for (int h = (B % 2 == 1) ? 2 : 1; h < M; h *= 4) {
-            const int step = 32 / (4 * h);  // W_4h^m = W_32^(m step)
+            for (int j = 0; j < h; ++j) {
+                const int tix = j * (32 / len);
+                float2 w = c_w32[tix];
+                if (sign > 0) w.y = -w.y;
 #pragma unroll
-            for (int s = 0; s < M; s += 4 * h) {
-#pragma unroll
-                for (int j = 0; j < h; ++j) {
-                    const float2 A = a[s + j];
-                    const float2 Bv = tw32_mul(a[s + j + h], 2 * j * step, sign);
-                    const float2 C = tw32_mul(a[s + j + 2 * h], j * step, sign);
-                    const float2 D = tw32_mul(a[s + j + 3 * h], 3 * j * step, sign);
-                    const float2 apb = cadd(A, Bv), amb = csub(A, Bv);
-                    const float2 cpd = cadd(C, D), rot = cmul_si(csub(C, D), sign);
-                    a[s + j] = cadd(apb, cpd);
-                    a[s + j + 2 * h] = csub(apb, cpd);
-                    a[s + j + h] = cadd(amb, rot);
-                    a[s + j + 3 * h] = csub(amb, rot);
+                for (int s = 0; s < M; s += len) {
+                    const float2 u = a[s + j];
+                    float2 t = a[s + j + h];
+                    if (tix == 8)
+                        t = cmul_si(t, sign);
+                    else if (tix != 0)
+                        t = cmul(t, w);
+                    a[s + j] = cadd(u, t);
+                    a[s + j + h] = csub(u, t);
                 }
             }
         }
