@@ -571,32 +571,29 @@ __device__ __forceinline__ void dep_one(uint32_t *acc, int off, float w, float w
 }
 
 // One particle of grid g for lane (a, b).
-// FAST (no tile spans a periodic axis): loc.x is the offset of the particle's
-// cell s ^ par for s = 0 in the stencil row (a, b) = (0, 0), relative to the
-// accumulator, with par the cell-order bit (cell 1 ^ par is at loc.x + 1 -
-// 2 par); row (a, b) adds a*kSI + b*kSJ (lane_off).  loc.y has bit 4a + b set
-// for the rows inside the tile and par in bit 31; the deposit reads these two
-// words only.  The 4 k cells are contiguous (kPadK columns take those beyond
-// the tile).
+// FAST (no tile spans a periodic axis): loc.x / loc.y are the offsets of the
+// particle's cells s ^ par for s = 0 and 1 in the stencil row (a, b) = (0, 0),
+// relative to the accumulator, with par the cell-order bit; row (a, b) adds
+// a*kSI + b*kSJ (lane_off).  loc.z has bit 4a + b set for the rows inside the
+// tile.  The 4 k cells are contiguous (kPadK columns take those beyond the tile).
 // Otherwise loc.x / loc.y hold the 4 local i / j indices as bytes (kOut outside
 // the tile) and loc.z the 4 padded k cells as bytes, in step order.
 // The k weights are stored in step order.
 template <bool WIDE, bool FAST, int GS>
 __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, int slot, int g, int a, int b,
                                             int lane_off) {
+    const uint4 loc = sb.loc[slot];
     const float w = reinterpret_cast<const float *>(&sb.w[0][slot])[a] *
                     reinterpret_cast<const float *>(&sb.w[1][slot])[b];
     const float4 wz = sb.w[2][slot];
     if (FAST) {
-        const uint2 loc = *reinterpret_cast<const uint2 *>(&sb.loc[slot]);
-        if (!((loc.y >> (4 * a + b)) & 1u)) return;  // a stencil row outside the tile
-        const int o0 = (int)loc.x + lane_off, o1 = o0 + 1 - 2 * (int)(loc.y >> 31);
+        if (!((loc.z >> (4 * a + b)) & 1u)) return;  // a stencil row outside the tile
+        const int o0 = (int)loc.x + lane_off, o1 = (int)loc.y + lane_off;
         dep_one<WIDE>(acc, o0, w, wz.x);
         dep_one<WIDE>(acc, o1, w, wz.y);
         dep_one<WIDE>(acc, o0 + 2, w, wz.z);
         dep_one<WIDE>(acc, o1 + 2, w, wz.w);
     } else {
-        const uint4 loc = sb.loc[slot];
         const uint32_t li = (loc.x >> (8 * a)) & 255u;
         const uint32_t lj = (loc.y >> (8 * b)) & 255u;
         if ((li | lj) >= 32u) return;  // kOut: a stencil row outside the tile
@@ -712,7 +709,7 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
                 const uint32_t mi = (unsigned)(lv[0] + 4) < 40u ? masktab[0][lv[0] + 4] : 0u;
                 const uint32_t mj = (unsigned)(lv[1] + 4) < 40u ? masktab[1][lv[1] + 4] : 0u;
                 const int b0 = gofs + lv[0] * kSI + lv[1] * kSJ + lv[2] + kPadK + (int)par;
-                loc = make_uint4((uint32_t)b0, (kmiss ? 0u : mi * mj) | (par << 31), 0u, 0u);
+                loc = make_uint4((uint32_t)b0, (uint32_t)(b0 + 1 - 2 * (int)par), kmiss ? 0u : mi * mj, 0u);
             } else {
                 uint32_t li, lj, lk;
                 li = cyc[0] ? pack_local(bgv[0], Ng, ts.t0[0], ts.te[0], kOut)
