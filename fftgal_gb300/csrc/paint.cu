@@ -614,9 +614,11 @@ __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, i
         for (int p = 0; p < np; ++p) deposit_one<WIDE, FAST, GS>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
     } else {
         // one grid: 32 particles staged in slots 0..31, the half warps
-        // deposit alternate ones (unrolled by 8: 10.90 ms against 11.18 by 4,
-        // 11.45 by 2 and 11.97 by 1, both grids at Ng = 1024)
-#pragma unroll 8
+        // deposit alternate ones; unrolled fully, so that the shared loads of
+        // later particles are issued among the atomics of earlier ones (10.65
+        // ms against 10.87 by 8, 11.18 by 4, 11.45 by 2 and 11.97 by 1, both
+        // grids at Ng = 1024)
+#pragma unroll 16
         for (int p = h; p < np; p += 2) deposit_one<WIDE, FAST, GS>(acc, sb, p, 0, a, b, lane_off);
     }
 }
