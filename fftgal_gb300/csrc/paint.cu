@@ -84,14 +84,12 @@ static_assert(kSI % 32 == 8 && kSJ % 32 == 6 && kGS % 2 == 1, "bank layout");
 constexpr int kAccWords = 2 * kGS > 32 * kSI ? 2 * kGS : 32 * kSI;
 static_assert(31 * kSI + 15 * kSJ + kSJ <= kAccWords, "32-row tile does not fit the layout");
 constexpr size_t kAccBytes = (sizeof(uint32_t) * kAccWords + 15) / 16 * 16;
-// the tile-paint CTA shape: 512 threads, two CTAs per SM, the two grids of
-// 16 i rows at stride kGS or one grid of 32 rows.  (One 1024-thread CTA per
-// SM holding both grids of 32-row tiles, 158 KB of sums, was measured slower
-// than two one-grid CTAs per SM.)
-template <int THREADS> struct PaintCfg;
-template <> struct PaintCfg<512> {
-    static constexpr int GS = kGS, ACC_WORDS = kAccWords, MINB = 2;
-};
+// The tile-paint CTA: 512 threads, two CTAs per SM, the two grids of 16 i
+// rows at stride kGS or one grid of 32 rows.  (One 1024-thread CTA per SM
+// holding both grids of 32-row tiles, 158 KB of sums, was measured slower than
+// two one-grid CTAs per SM.)  A dense tile's 64-bit sums hold 16 i rows.
+constexpr int kWideRows = kAccWords / 2 / kSI;
+static_assert(kWideRows == 16, "64-bit rows");
 // largest fixed-point scale: products stay below 2^22 so the FMA trick of
 // deposit4 converts them to integers exactly
 constexpr int kMaxFixBits = 23;
@@ -579,7 +577,7 @@ __device__ __forceinline__ void dep_one(uint32_t *acc, int off, float w, float w
 // Otherwise loc.x / loc.y hold the 4 local i / j indices as bytes (kOut outside
 // the tile) and loc.z the 4 padded k cells as bytes, in step order.
 // The k weights are stored in step order.
-template <bool WIDE, bool FAST, int GS>
+template <bool WIDE, bool FAST>
 __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, int slot, int g, int a, int b,
                                             int lane_off) {
     const uint4 loc = sb.loc[slot];
@@ -597,7 +595,7 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
         const uint32_t li = (loc.x >> (8 * a)) & 255u;
         const uint32_t lj = (loc.y >> (8 * b)) & 255u;
         if ((li | lj) >= 32u) return;  // kOut: a stencil row outside the tile
-        const int row = g * GS + (int)(li * kSI + lj * kSJ);
+        const int row = g * kGS + (int)(li * kSI + lj * kSJ);
         dep_one<WIDE>(acc, row + (int)(loc.z & 255u), w, wz.x);
         dep_one<WIDE>(acc, row + (int)((loc.z >> 8) & 255u), w, wz.y);
         dep_one<WIDE>(acc, row + (int)((loc.z >> 16) & 255u), w, wz.z);
@@ -605,13 +603,13 @@ __device__ __forceinline__ void deposit_one(uint32_t *acc, const StageBuf &sb, i
     }
 }
 
-template <bool WIDE, bool FAST, int GS>
+template <bool WIDE, bool FAST>
 __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, int np, int ngr, int lane) {
     const int h = lane >> 4, a = (lane >> 2) & 3, b = lane & 3;
     const int lane_off = a * kSI + b * kSJ;
     if (ngr > 1) {
 #pragma unroll 4
-        for (int p = 0; p < np; ++p) deposit_one<WIDE, FAST, GS>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
+        for (int p = 0; p < np; ++p) deposit_one<WIDE, FAST>(acc, sb, stage_slot(p, h), h, a, b, lane_off);
     } else {
         // one grid: 32 particles staged in slots 0..31, the half warps
         // deposit alternate ones; unrolled fully, so that the shared loads of
@@ -619,7 +617,7 @@ __device__ __forceinline__ void deposit_all(uint32_t *acc, const StageBuf &sb, i
         // ms against 10.87 by 8, 11.18 by 4, 11.45 by 2 and 11.97 by 1, both
         // grids at Ng = 1024)
 #pragma unroll 16
-        for (int p = h; p < np; p += 2) deposit_one<WIDE, FAST, GS>(acc, sb, p, 0, a, b, lane_off);
+        for (int p = h; p < np; p += 2) deposit_one<WIDE, FAST>(acc, sb, p, 0, a, b, lane_off);
     }
 }
 
@@ -642,7 +640,7 @@ __device__ __forceinline__ int fix_bits_for(uint32_t n) {
 // g1 (NGS = 1), then deposits them, into 32-bit sums or (WIDE) the 64-bit sums
 // of grid g1; the records of the warp's next batch are loaded before the
 // deposit so their latency hides behind it
-template <int NGS, bool WIDE, int THREADS>
+template <int NGS, bool WIDE>
 __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const uint4 *__restrict__ sorted,
                                               const uint32_t *seg_begin, const uint32_t *seg_pref,
                                               const TileSegs &ts, const PaintParams &pp, const bool *cyc,
@@ -650,10 +648,10 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
                                               const uint32_t (*masktab)[40], int lane, int warp) {
     const int Ng = pp.Ng, fb = pp.fb, nseg = ts.nseg;
     const uint32_t total = ts.total;
-    constexpr int nwarp = THREADS / 32, GS = PaintCfg<THREADS>::GS;
+    constexpr int nwarp = kPaintThreads / 32;
     const int parts = NGS > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
     const int gs = NGS > 1 ? lane / kStageParts : g1;             // the grid this lane stages
-    const int gofs = (WIDE || NGS == 1) ? 0 : gs * GS;            // and its accumulator
+    const int gofs = (WIDE || NGS == 1) ? 0 : gs * kGS;           // and its accumulator
     const uint32_t bstride = (uint32_t)nwarp * parts;
     uint32_t base = (uint32_t)warp * parts;
     uint4 rec = make_uint4(0, 0, 0, 0);
@@ -735,9 +733,9 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
         }
         const int np = min((uint32_t)parts, total - base);
         if (fast)
-            deposit_all<WIDE, true, GS>(acc, sb, np, NGS, lane);
+            deposit_all<WIDE, true>(acc, sb, np, NGS, lane);
         else
-            deposit_all<WIDE, false, GS>(acc, sb, np, NGS, lane);
+            deposit_all<WIDE, false>(acc, sb, np, NGS, lane);
         __syncwarp();
     }
 }
@@ -748,21 +746,16 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
 // next batch of records before depositing the current one.
 // NGR = pp.ngrids (1 or 2), a template parameter so that the staging and
 // deposit loops are specialised for one grid or the interlaced pair.
-template <int NGR, int THREADS>
-__global__ void __launch_bounds__(THREADS, PaintCfg<THREADS>::MINB)
+template <int NGR>
+__global__ void __launch_bounds__(kPaintThreads, 2)
 paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 *__restrict__ sorted,
                   PaintOut po, unsigned ntiles, int gsplit) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int GS = PaintCfg<THREADS>::GS;
-    constexpr int ACC_BYTES = (4 * PaintCfg<THREADS>::ACC_WORDS + 15) / 16 * 16;
-    // rows of 64-bit sums that the accumulators hold (a dense tile's pass)
-    constexpr int WROWS = PaintCfg<THREADS>::ACC_WORDS / 2 / kSI;
-    static_assert(WROWS == 16 || WROWS == 32, "wide rows");
-    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                 // [2][GS]
-    StageBuf *stage = reinterpret_cast<StageBuf *>(smem_raw + ACC_BYTES);  // [warps]
+    uint32_t *acc = reinterpret_cast<uint32_t *>(smem_raw);                 // [2][kGS]
+    StageBuf *stage = reinterpret_cast<StageBuf *>(smem_raw + kAccBytes);  // [warps]
     // the per-block counts and their window sums (before pass B) use the stage area
     uint32_t *blk = reinterpret_cast<uint32_t *>(stage) + kBlkN;  // [kBlkN]
-    static_assert(2 * kBlkN * sizeof(uint32_t) <= sizeof(StageBuf) * (THREADS / 32), "block counts");
+    static_assert(2 * kBlkN * sizeof(uint32_t) <= sizeof(StageBuf) * (kPaintThreads / 32), "block counts");
     __shared__ uint32_t seg_begin[kMaxSeg];
     __shared__ uint32_t seg_pref[kMaxSeg + 1];
     __shared__ uint32_t scan_ws[33];
@@ -797,7 +790,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     };
 
     const int Ng = pp.Ng, ngr = NGR;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = THREADS / 32;  // launched with THREADS
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kPaintThreads / 32;  // launched with kPaintThreads
     // gsplit (NGR = 1 with pp.ngrids = 2): even CTAs paint grid 0 and odd
     // CTAs grid 1 of the same tiles, from one sort keyed for both grids
     const int mg = (NGR == 1 && gsplit) ? (int)(blockIdx.x & 1) : 0;  // the grid of a one-grid CTA
@@ -805,7 +798,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
     const unsigned ncta = (NGR == 1 && gsplit) ? gridDim.x >> 1 : gridDim.x;
     unsigned tile = cta;
     if (tile >= ntiles) return;
-    for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
+    for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
         reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
     TileSegs ts;
     {
@@ -832,9 +825,9 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             int nb[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a) nb[a] = cyc[a] ? (Ng + kBlk - 1) / kBlk : blk_dim(a);
-            for (int e = tid; e < kBlkN; e += THREADS) blk[e] = 0u;
+            for (int e = tid; e < kBlkN; e += kPaintThreads) blk[e] = 0u;
             __syncthreads();
-            for (uint32_t q = tid; q < total; q += THREADS) {
+            for (uint32_t q = tid; q < total; q += kPaintThreads) {
                 const uint4 r = sorted[seg_index(q, seg_begin, seg_pref, nseg)];
                 const uint32_t rw[3] = {r.x, r.y, r.z};
                 int bidx = 0;
@@ -863,7 +856,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             // reuses the stage area.
             uint32_t *tmp = reinterpret_cast<uint32_t *>(stage);
             const int D1 = blk_dim(1), D2 = blk_dim(2);
-            for (int e = tid; e < kBlkN; e += THREADS) {
+            for (int e = tid; e < kBlkN; e += kPaintThreads) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 uint32_t v = 0;
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[2] || k + 2 < nb[2]);
@@ -872,7 +865,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                 tmp[e] = v;
             }
             __syncthreads();
-            for (int e = tid; e < kBlkN; e += THREADS) {
+            for (int e = tid; e < kBlkN; e += kPaintThreads) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 uint32_t v = 0;
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[1] || j + 2 < nb[1]);
@@ -882,7 +875,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             }
             __syncthreads();
             uint32_t mx = 0;
-            for (int e = tid; e < kBlkN; e += THREADS) {
+            for (int e = tid; e < kBlkN; e += kPaintThreads) {
                 const int k = e % D2, j = (e / D2) % D1, i = e / (D2 * D1);
                 const bool in = i < nb[0] && j < nb[1] && k < nb[2] && (cyc[0] || i + 2 < nb[0]);
                 if (in) {
@@ -907,13 +900,13 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
         // a 32-row tile at a time: 16 rows of 64-bit sums fill the shared
         // memory); otherwise one pass paints every grid into 32-bit sums
         const bool wide = fixbits < kWideBelow;
-        const int nhalf = (wide && ts.te[0] > WROWS) ? 2 : 1;
+        const int nhalf = (wide && ts.te[0] > kWideRows) ? 2 : 1;
         const int npass = wide ? ngr * nhalf : 1;
         const float fscale = ldexpf(1.0f, wide ? kWideBits : fixbits);
         if (wide) {
             // the 32-bit tiles leave sums in the row padding: clear all of it
             __syncthreads();
-            for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
+            for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
                 reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
             __syncthreads();
         }
@@ -926,15 +919,15 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
             TileSegs tv = ts;             // and its rows
             if (nhalf == 2) {
                 const int ph = pass % nhalf;
-                tv.t0[0] = ts.t0[0] + WROWS * ph;
-                tv.te[0] = ph ? ts.te[0] - WROWS : WROWS;
+                tv.t0[0] = ts.t0[0] + kWideRows * ph;
+                tv.te[0] = ph ? ts.te[0] - kWideRows : kWideRows;
                 build_tabs(tv.te[0], tv.te[1]);
             }
             if (wide)
-                paint_records<1, true, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
+                paint_records<1, true>(acc, stage[warp], sorted, seg_begin, seg_pref, tv, pp, cyc, fast, fscale, pg,
                                        loctab, masktab, lane, warp);
             else
-                paint_records<NGR, false, THREADS>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale,
+                paint_records<NGR, false>(acc, stage[warp], sorted, seg_begin, seg_pref, ts, pp, cyc, fast, fscale,
                                                    mg, loctab, masktab, lane, warp);
             __syncthreads();
 
@@ -973,7 +966,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                         }
                     }
                     __syncthreads();
-                    for (int e = tid; e < (ACC_BYTES / 16); e += THREADS)
+                    for (int e = tid; e < (int)(kAccBytes / 16); e += kPaintThreads)
                         reinterpret_cast<uint4 *>(smem_raw)[e] = make_uint4(0, 0, 0, 0);
                     __syncthreads();
                     continue;
@@ -986,7 +979,7 @@ paint_coop_kernel(PaintParams pp, const uint32_t *__restrict__ off, const uint4 
                     float *o0 = reinterpret_cast<float *>(po.out[mg]) + obase + li * istride;
                     float *o1 = ngr > 1 ? reinterpret_cast<float *>(po.out[1]) + obase + li * istride : nullptr;
                     uint32_t *a0 = acc + kPadK + li * kSI;
-                    uint32_t *a1 = a0 + GS;
+                    uint32_t *a1 = a0 + kGS;
                     for (int lj = 0; lj < te1; ++lj, o0 += rstride, o1 += rstride, a0 += kSJ, a1 += kSJ) {
                         // padding cells take 0 x scale, as the reference scales the
                         // whole padded grid (src/fft.c:127-129): NaN for an empty catalog
@@ -1276,10 +1269,8 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
         // both grids' stencils); else both grids of 16-row tiles per CTA
         constexpr int T = kPaintThreads;
         const size_t smem = kAccBytes + sizeof(StageBuf) * (T / 32);
-        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        FG_CUDA(cudaFuncSetAttribute(paint_coop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const int split = big && ngrids == 2;
         unsigned nb = (unsigned)((cta_per_sm == 1 ? 1 : 2) * num_sms());
         if (split) {
@@ -1289,9 +1280,9 @@ int paint(const PaintTiling *t, PaintScratch *s, int grid_prec, const void *x, c
             nb = nb < ntiles ? nb : ntiles;
         }
         if (ngrids == 1 || split)
-            paint_coop_kernel<1, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles, split);
+            paint_coop_kernel<1><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles, split);
         else
-            paint_coop_kernel<2, T><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles, 0);
+            paint_coop_kernel<2><<<nb, T, smem, st>>>(pp, s->hist, (const uint4 *)s->sorted, po, ntiles, 0);
     } else {
         const size_t smem = (size_t)ngrids * kT3 * sizeof(double);
         FG_CUDA(cudaFuncSetAttribute(paint_tile_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
