@@ -51,3 +51,17 @@ def test_relaunch_command():
             os.environ.pop("WORLD_SIZE", None)
         else:
             os.environ["WORLD_SIZE"] = saved
+
+
+def test_algorithmic_bytes_of_the_stages():
+    """The per-stage algorithmic bytes behind the bench line's GB/s and HBM
+    fractions (Ng = 1024, Np = 1e8): the lazy fused call's finish + binning
+    reads both grids and stores nothing; the FFT passes read and write both."""
+    import bench
+    a = bench.algorithmic_bytes(1024, 100_000_000)
+    G4 = 1024 * 1024 * 1026 * 4
+    assert a["paint_key"] == 12 * 100_000_000
+    assert a["paint_scatter"] == 28 * 100_000_000
+    assert a["paint_tile"] == 16 * 100_000_000 + 2 * G4
+    assert a["fft_j"] == a["fft_i"] == 4 * G4
+    assert a["finish_bin"] == 2 * G4
