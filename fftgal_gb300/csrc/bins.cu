@@ -420,7 +420,7 @@ bin_power_slab_kernel(BinDev d, const float2 *__restrict__ f, SlabFinish fin, fl
             }
             const long estep = rows_i ? (long)Ng * nh : (long)nh;  // elements between consecutive rows
             long e = (rows_i ? ((long)r0 * Ng + fixed) : ((long)fixed * Ng + r0)) * nh + k;
-#pragma unroll 4
+#pragma unroll 8
             for (int r = 0; r < kSlabJ; ++r, e += estep) {
                 float2 phr = make_float2(0.f, 0.f);
                 float wr = 0.f;

@@ -652,6 +652,7 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
     const int parts = NGS > 1 ? kStageParts : 2 * kStageParts;  // particles per warp and round
     const int gs = NGS > 1 ? lane / kStageParts : g1;             // the grid this lane stages
     const int gofs = (WIDE || NGS == 1) ? 0 : gs * kGS;           // and its accumulator
+    const float inv = __int_as_float((127 - fb) << 23);            // 2^-fb (fb <= 24)
     const uint32_t bstride = (uint32_t)nwarp * parts;
     uint32_t base = (uint32_t)warp * parts;
     uint4 rec = make_uint4(0, 0, 0, 0);
@@ -668,7 +669,6 @@ __device__ __forceinline__ void paint_records(uint32_t *acc, StageBuf &sb, const
         float4 wk = make_float4(0.f, 0.f, 0.f, 0.f);
         if (valid) {
             const uint32_t rw[3] = {rec.x, rec.y, rec.z};
-            const float inv = ldexpf(1.0f, -fb);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const int b0 = (int)(rw[a] >> fb);
